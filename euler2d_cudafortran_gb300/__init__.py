@@ -1,0 +1,268 @@
+"""GB300-native Euler-2D explicit step (pkestene/euler2d_cudaFortran hot path).
+
+Python host mirror of the reference's ``m_run`` module procedures, calling the
+C ABI of ``libeuler2d_gb300.so`` (include/euler2d_gb300.h) through ctypes:
+
+=====================================  =========================================
+reference (serial_ref/m_run.f90)       here
+=====================================  =========================================
+initHydroParameters + run_init :48,150 ``HydroRun(params)``
+init_implode :524                      ``HydroRun.init_implode()``
+compute_dt(params, dt, useU) :248      ``HydroRun.compute_dt(useU)``
+make_boundaries(params, data) :561     ``HydroRun.make_boundaries(which)``
+godunov_unsplit(nStep, dt) :187        ``HydroRun.godunov_unsplit(nStep, dt)``
+main.f90:53-76 loop (no I/O)           ``HydroRun.advance(nStep0, nsteps)``
+saveVTK(data, iStep) :653              ``vtk.save_vtk(...)``
+run_cleanup :172                       ``HydroRun.close()``
+=====================================  =========================================
+
+There is no CPU fallback: every call runs the CUDA library, and importing the
+wrapper fails loudly if the library was not built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .namelist import RunConfig, read_config  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libeuler2d_gb300.so")
+
+E2D_OK = 0
+E2D_ERR_INVALID_ARG = 1
+E2D_ERR_CUDA = 2
+E2D_ERR_OOM = 3
+E2D_ERR_NUMERICS = 4
+E2D_ERR_NO_DEVICE = 5
+HEALTH_DT_NONFINITE = 1
+HEALTH_NEG_DENSITY = 2
+HEALTH_TMA_TIMEOUT = 4
+RIEMANN_APPROX = 0
+RIEMANN_HLLC = 2
+
+EXPORTED_SYMBOLS = [
+    "e2d_default_params", "e2d_create", "e2d_destroy", "e2d_get_sizes", "e2d_set_stream", "e2d_synchronize",
+    "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
+    "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
+    "e2d_get_health", "e2d_last_error", "e2d_device_state",
+]
+
+
+class E2DError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"euler2d_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    """struct e2d_params of include/euler2d_gb300.h."""
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("smallr", ctypes.c_double), ("smallc", ctypes.c_double),
+        ("niter_riemann", ctypes.c_int), ("iorder", ctypes.c_int), ("slope_type", ctypes.c_int),
+        ("boundary_type_xmin", ctypes.c_int), ("boundary_type_xmax", ctypes.c_int),
+        ("boundary_type_ymin", ctypes.c_int), ("boundary_type_ymax", ctypes.c_int),
+        ("implementation_version", ctypes.c_int), ("riemann_solver", ctypes.c_int),
+        ("precision", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m euler2d_cudafortran_gb300.build` "
+                          "(there is no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    vp, ip, i, d = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_double
+    sig = {
+        "e2d_default_params": [ctypes.POINTER(Params)],
+        "e2d_create": [ctypes.POINTER(Params), ctypes.POINTER(vp)],
+        "e2d_destroy": [vp],
+        "e2d_get_sizes": [vp, ip, ip, ctypes.POINTER(ctypes.c_size_t)],
+        "e2d_set_stream": [vp, vp],
+        "e2d_synchronize": [vp],
+        "e2d_init_implode": [vp],
+        "e2d_init_diagonal": [vp, d, d, d, d, d],
+        "e2d_upload_state": [vp, i, vp],
+        "e2d_download_state": [vp, i, vp],
+        "e2d_compute_dt": [vp, i, vp],
+        "e2d_make_boundaries": [vp, i],
+        "e2d_godunov_unsplit": [vp, i, d],
+        "e2d_advance": [vp, i, i, vp],
+        "e2d_last_advance_ms": [vp, ctypes.POINTER(ctypes.c_float)],
+        "e2d_get_invdt": [vp, ctypes.POINTER(ctypes.c_double)],
+        "e2d_get_health": [vp, ctypes.POINTER(ctypes.c_uint)],
+        "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
+                             ctypes.POINTER(ctypes.c_size_t)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    lib.e2d_last_error.argtypes = []
+    lib.e2d_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != E2D_OK:
+        raise E2DError(rc, load_library().e2d_last_error().decode())
+
+
+def default_params() -> Params:
+    p = Params()
+    _check(load_library().e2d_default_params(ctypes.byref(p)))
+    return p
+
+
+def params_from_config(cfg: RunConfig) -> Params:
+    p = default_params()
+    for k in ("nx", "ny", "gamma0", "cfl", "smallr", "smallc", "niter_riemann", "iorder", "slope_type",
+              "boundary_type_xmin", "boundary_type_xmax", "boundary_type_ymin", "boundary_type_ymax",
+              "riemann_solver", "precision"):
+        setattr(p, k, getattr(cfg, k))
+    p.implementation_version = cfg.implementationVersion
+    return p
+
+
+def make_params(**kw) -> Params:
+    p = default_params()
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise TypeError(f"unknown parameter {k}")
+        setattr(p, k, v)
+    return p
+
+
+class HydroRun:
+    """One run on the current CUDA device: u, u2 and the step's work arrays."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self._lib = load_library()
+        self.params = params if params is not None else make_params(**kw)
+        h = ctypes.c_void_p()
+        _check(self._lib.e2d_create(ctypes.byref(self.params), ctypes.byref(h)))
+        self._h = h
+        isz, jsz, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+        _check(self._lib.e2d_get_sizes(h, ctypes.byref(isz), ctypes.byref(jsz), ctypes.byref(nb)))
+        self.isize, self.jsize, self.state_bytes = isz.value, jsz.value, nb.value
+        self.dtype = np.float64 if self.params.precision == 8 else np.float32
+
+    # -- lifecycle -------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.e2d_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state -----------------------------------------------------------
+    def new_state(self) -> np.ndarray:
+        return np.zeros((4, self.jsize, self.isize), dtype=self.dtype)
+
+    def init_implode(self):
+        _check(self._lib.e2d_init_implode(self._h))
+
+    def init_diagonal(self, offset, rho_hi, p_hi, rho_lo, p_lo):
+        _check(self._lib.e2d_init_diagonal(self._h, offset, rho_hi, p_hi, rho_lo, p_lo))
+
+    def set_state(self, which: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.shape != (4, self.jsize, self.isize):
+            raise ValueError(f"state must have shape (4, {self.jsize}, {self.isize})")
+        _check(self._lib.e2d_upload_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
+
+    def get_state(self, which: int) -> np.ndarray:
+        a = self.new_state()
+        _check(self._lib.e2d_download_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
+        return a
+
+    # -- the reference procedures -----------------------------------------
+    def compute_dt(self, useU: int) -> float:
+        dt = (ctypes.c_double if self.params.precision == 8 else ctypes.c_float)()
+        _check(self._lib.e2d_compute_dt(self._h, useU, ctypes.byref(dt)))
+        return dt.value
+
+    def make_boundaries(self, which: int):
+        _check(self._lib.e2d_make_boundaries(self._h, which))
+
+    def godunov_unsplit(self, nStep: int, dt: float):
+        _check(self._lib.e2d_godunov_unsplit(self._h, nStep, float(dt)))
+
+    def advance(self, nStep0: int, nsteps: int, log: bool = True):
+        buf = np.zeros(max(nsteps, 1), dtype=self.dtype) if log else None
+        ptr = buf.ctypes.data_as(ctypes.c_void_p) if log else None
+        _check(self._lib.e2d_advance(self._h, nStep0, nsteps, ptr))
+        return buf[:nsteps] if log else None
+
+    def last_advance_ms(self) -> float:
+        ms = ctypes.c_float()
+        _check(self._lib.e2d_last_advance_ms(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        _check(self._lib.e2d_synchronize(self._h))
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(self._lib.e2d_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def invdt(self) -> float:
+        x = ctypes.c_double()
+        _check(self._lib.e2d_get_invdt(self._h, ctypes.byref(x)))
+        return x.value
+
+    def health(self) -> int:
+        x = ctypes.c_uint()
+        _check(self._lib.e2d_get_health(self._h, ctypes.byref(x)))
+        return x.value
+
+    def final_state(self, nsteps: int) -> np.ndarray:
+        """The state after nsteps steps from u: u if nsteps is even, else u2."""
+        return self.get_state(nsteps % 2)
+
+
+def run_steps(nsteps: int, params: Params | None = None, u0: np.ndarray | None = None,
+              mode: str = "advance", **kw):
+    """The serial_ref/main.f90 loop (no output) on the GPU.
+
+    mode="advance": one e2d_advance call (device-resident dt, graph replay).
+    mode="percall": compute_dt / godunov_unsplit per step, as main.f90 calls them.
+    Returns (final_state, dt_log)."""
+    with HydroRun(params, **kw) as run:
+        if u0 is None:
+            run.init_implode()
+        else:
+            run.set_state(0, u0)
+        if mode == "advance":
+            dts = run.advance(0, nsteps)
+        else:
+            dt = run.compute_dt(0)
+            run.make_boundaries(0)
+            dts = []
+            for n in range(nsteps):
+                dt = run.compute_dt(n % 2)
+                run.godunov_unsplit(n, dt)
+                dts.append(dt)
+            dts = np.array(dts, dtype=run.dtype)
+        return run.final_state(nsteps), dts

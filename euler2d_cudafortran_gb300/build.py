@@ -1,0 +1,87 @@
+"""Build of the native parts: the CUDA library (sm_103a) and the C++ HydroRun driver.
+
+Everything is built in-tree under ``euler2d_cudafortran_gb300/_build/`` with
+plain ``nvcc``/``g++`` invocations run in parallel (no cmake), so the same
+recipe works on x86-64 (cross-compiling the device code) and on the aarch64
+GPU host.
+
+Numerics flags: ``-fmad=false`` stops the compiler from contracting a multiply
+and an add into one FMA, and ``-prec-div=true -prec-sqrt=true -ftz=false`` keep
+IEEE round-to-nearest division and square root in single precision (double is
+always IEEE).  Host code gets ``-ffp-contract=off`` for the same reason.  With
+these, every operation of the step rounds as in the reference's Fortran build.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+DRIVER = os.path.join(HERE, "driver")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libeuler2d_gb300.so")
+EXE = os.path.join(OUT, "euler2d_gb300")
+
+CUDA_SOURCES = ["abi.cu", "k_sweeps.cu", "k_fused.cu"]
+DRIVER_SOURCES = ["main.cpp", "namelist.cpp", "vtk.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
+                     "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", os.path.join(ROOT, "include")]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _run(cmd):
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
+    return res.stdout + res.stderr
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
+    """Compile the CUDA library and the driver; returns the library path."""
+    os.makedirs(OUT, exist_ok=True)
+    nvcc = _nvcc()
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(ROOT, "include", "euler2d_gb300.h"))
+    flags = NVCC_FLAGS + (extra_flags or [])
+    jobs = []
+    objs = []
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OUT, src.replace(".cu", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + headers + [__file__]):
+            jobs.append([nvcc] + flags + ["-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out.strip():
+                print(out)
+    if _stale(LIB, objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs)
+    drv = [os.path.join(DRIVER, f) for f in DRIVER_SOURCES]
+    if all(os.path.exists(d) for d in drv) and _stale(EXE, drv + [LIB, os.path.join(DRIVER, "namelist.h")]):
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-o", EXE]
+             + drv + ["-L", OUT, "-leuler2d_gb300", "-Wl,-rpath,$ORIGIN"])
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print(LIB)

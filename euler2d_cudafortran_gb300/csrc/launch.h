@@ -1,0 +1,64 @@
+// launch.h -- host-side launchers shared by the translation units of the library.
+#pragma once
+#include <cuda_runtime.h>
+#include "physics.cuh"
+
+namespace e2d {
+
+// Small device control block of a run: running CFL maxima (two slots, so a
+// step can read one while its update kernel folds the next state's maximum
+// into the other), health flags and the device dt log.
+struct Ctl {
+  unsigned long long inv64[2];  // FP64 runs: bit images of invDt (non-negative)
+  unsigned int inv32[2];        // FP32 runs
+  unsigned int health;          // E2D_HEALTH_* bits
+  unsigned int pad;
+};
+
+template <typename Real> __host__ __device__ inline Real* inv_slot(Ctl* c, int s);
+template <> __host__ __device__ inline double* inv_slot<double>(Ctl* c, int s) { return reinterpret_cast<double*>(&c->inv64[s]); }
+template <> __host__ __device__ inline float* inv_slot<float>(Ctl* c, int s) { return reinterpret_cast<float*>(&c->inv32[s]); }
+
+// Where a step kernel takes its dt from: a host value (godunov_unsplit called
+// with dt, as serial_ref/main.f90:72) or the running maximum on the device
+// (dt = cfl / invDt, serial_ref/m_run.f90:308), logged to dt_log[log_index].
+template <typename Real>
+struct StepDt {
+  Real dt_value;
+  int from_slot;    // 1: dt = cfl / inv[rd_slot]
+  int rd_slot;      // slot holding the running max for this step's dt
+  int wr_slot;      // slot receiving max(inv[rd], max over the new state); -1: no reduction
+  Real* dt_log;     // device; may be null
+  int log_index;
+};
+
+// ---- k_sweeps.cu ----
+template <typename Real> void launch_init_diagonal(const Hydro<Real>& h, Field<Real> u, double offset, double rho_hi,
+                                                   double p_hi, double rho_lo, double p_lo, cudaStream_t s);
+template <typename Real> void launch_boundaries(const Hydro<Real>& h, Field<Real> u, cudaStream_t s);
+// Reduce the CFL maximum of u into ctl->inv[slot] (atomic max; running max kept).
+template <typename Real> void launch_dt_reduce(const Hydro<Real>& h, Field<Real> u, Ctl* ctl, int slot, cudaStream_t s);
+template <typename Real> void launch_prim(const Hydro<Real>& h, Field<Real> u, Field<Real> q, cudaStream_t s);
+// implementationVersion 2: fluxes stored (serial_ref computeAndStoreFluxes + updateHydro)
+template <typename Real> void launch_fluxes_v2(const Hydro<Real>& h, Field<Real> q, StepDt<Real> sd, Ctl* ctl,
+                                               Field<Real> fx, Field<Real> fy, cudaStream_t s);
+template <typename Real> void launch_update_v2(const Hydro<Real>& h, Field<Real> in, Field<Real> fx, Field<Real> fy,
+                                               Field<Real> out, StepDt<Real> sd, Ctl* ctl, cudaStream_t s);
+// implementationVersion 1: face states stored, then fluxes + update in one tiled kernel
+template <typename Real> void launch_trace_v1(const Hydro<Real>& h, Field<Real> q, StepDt<Real> sd, Ctl* ctl,
+                                              Field<Real> qxm, Field<Real> qxp, Field<Real> qym, Field<Real> qyp,
+                                              cudaStream_t s);
+template <typename Real> void launch_flux_update_v1(const Hydro<Real>& h, Field<Real> in, Field<Real> qxm,
+                                                    Field<Real> qxp, Field<Real> qym, Field<Real> qyp,
+                                                    Field<Real> out, StepDt<Real> sd, Ctl* ctl, cudaStream_t s);
+
+// ---- k_fused.cu ---- implementationVersion 0: one fused kernel per step.
+// Builds (once per state buffer) the TMA descriptor of a state.
+struct FusedPlan;
+template <typename Real> FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2);
+void fused_plan_destroy(FusedPlan* p);
+template <typename Real> void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in,
+                                           Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
+                                           cudaStream_t s);
+
+}  // namespace e2d

@@ -1,0 +1,142 @@
+/*
+ * euler2d_gb300.h -- C ABI of the GB300 (sm_103a) Euler-2D explicit step.
+ *
+ * This is the drop-in boundary for the hot path of pkestene/euler2d_cudaFortran:
+ * the CFL time-step reduction (compute_dt) and the unsplit second-order Godunov
+ * update (make_boundaries, convertToPrimitives, computeAndStoreFluxes,
+ * updateHydro).  Each entry point replaces one module procedure of
+ * serial_ref/m_run.f90 (or cuf/m_HydroRun_gpu.cuf) called by the HydroRun
+ * driver serial_ref/main.f90; the procedure it replaces is cited beside it.
+ *
+ * Conventions
+ *  - Plain C types only; callable from Fortran through ISO_C_BINDING
+ *    (bind(C), type(c_ptr) handles, real(c_double)/real(c_float) arrays).
+ *  - Host state arrays use the Fortran layout A(isize, jsize, 4), column-major,
+ *    isize = nx+4, jsize = ny+4, variables ID=rho, IP=E, IU=rho*u, IV=rho*v
+ *    (serial_ref/m_constants.f90:11-14), element type double (precision 8) or
+ *    float (precision 4).
+ *  - The state pair u/u2 is selected by `which` / `useU`: 0 = u, 1 = u2, the
+ *    ping-pong of serial_ref/m_run.f90:197-201 (even nStep reads u, writes u2).
+ *  - Every function returns an int status (E2D_OK on success).  The reference
+ *    has no error codes; it stops on a bad namelist (serial_ref/m_run.f90:77-82,
+ *    cuf/m_HydroParameters.cuf:128-132), which maps to E2D_ERR_INVALID_ARG here.
+ *  - All device work is issued on the run's stream (e2d_set_stream); calls that
+ *    return host data synchronise that stream.
+ */
+#ifndef EULER2D_GB300_H
+#define EULER2D_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define E2D_OK 0
+#define E2D_ERR_INVALID_ARG 1
+#define E2D_ERR_CUDA 2
+#define E2D_ERR_OOM 3
+#define E2D_ERR_NUMERICS 4 /* dt non-finite: the run has blown up */
+#define E2D_ERR_NO_DEVICE 5
+
+/* Health flags (e2d_get_health). */
+#define E2D_HEALTH_DT_NONFINITE 1u
+#define E2D_HEALTH_NEG_DENSITY 2u /* a new conservative density was <= 0 or non-finite */
+
+#define E2D_RIEMANN_APPROX 0 /* riemann_2d, serial_ref/m_utils.f90:349 (the reference's choice) */
+#define E2D_RIEMANN_HLLC 2   /* riemann_2d_hllc, serial_ref/m_utils.f90:534 */
+
+/* Parameters: the &RUN-independent fields of type HydroPar
+ * (serial_ref/m_parameters.f90:10-36) as read by initHydroParameters
+ * (serial_ref/m_run.f90:48-128), plus the cuf namelist key
+ * implementationVersion (cuf/m_HydroParameters.cuf:90) and two keys of the
+ * trailing &GB300 namelist group. */
+typedef struct e2d_params {
+  int nx, ny;
+  double gamma0, cfl, smallr, smallc;
+  int niter_riemann, iorder, slope_type;
+  int boundary_type_xmin, boundary_type_xmax, boundary_type_ymin, boundary_type_ymax;
+  int implementation_version; /* 0 fused recompute, 1 stored prim + face states, 2 stored prim + fluxes */
+  int riemann_solver;         /* E2D_RIEMANN_APPROX or E2D_RIEMANN_HLLC */
+  int precision;              /* 8 = FP64 (fp_kind = dp_kind), 4 = FP32 (sp_kind) */
+} e2d_params;
+
+typedef struct e2d_run e2d_run; /* opaque run handle: owns u, u2 and work arrays on one GPU */
+
+/* Fill *p with the reference defaults of serial_ref/test.nml and
+ * serial_ref/m_parameters.f90 (niter_riemann=10, reflective walls), FP64,
+ * implementationVersion 0, approximate Riemann solver. */
+int e2d_default_params(e2d_params* p);
+
+/* initHydroParameters + run_init allocation (serial_ref/m_run.f90:48-128,150-158;
+ * cuf/m_HydroRun_gpu.cuf:83-118).  Validates p, allocates u, u2 (zeroed, as fresh
+ * allocate() pages) and the work arrays of the chosen implementation version on
+ * the current CUDA device.  The running CFL maximum starts at 0. */
+int e2d_create(const e2d_params* p, e2d_run** out);
+
+/* run_cleanup (serial_ref/m_run.f90:172-182). Accepts NULL. */
+int e2d_destroy(e2d_run* h);
+
+/* Sizes of the run: isize, jsize and bytes of one host state array. */
+int e2d_get_sizes(const e2d_run* h, int* isize, int* jsize, size_t* state_bytes);
+
+/* Issue all later device work on `stream` (a cudaStream_t; NULL = legacy default). */
+int e2d_set_stream(e2d_run* h, void* stream);
+int e2d_synchronize(e2d_run* h);
+
+/* init_implode (serial_ref/m_run.f90:524-555) on the device into u. */
+int e2d_init_implode(e2d_run* h);
+/* Generalised diagonal interface (high state where tmp > offset); offset 0.5,
+ * (1,1) / (0.125, (double)0.14f) is init_implode. */
+int e2d_init_diagonal(e2d_run* h, double offset, double rho_hi, double p_hi, double rho_lo,
+                      double p_lo);
+
+/* Host <-> device copies of u (which=0) or u2 (which=1), full arrays incl. ghosts. */
+int e2d_upload_state(e2d_run* h, int which, const void* host);
+int e2d_download_state(e2d_run* h, int which, void* host);
+
+/* compute_dt (serial_ref/m_run.f90:248-312; cuf/m_HydroRun_gpu.cuf:198-300):
+ * folds max over [3, size-3]^2 of (c+|u|)/dx + (c+|v|)/dy of u (useU=0) or u2
+ * (useU=1) into the run's running maximum and returns dt = cfl / max in *dt
+ * (a double* for precision 8, a float* for precision 4). */
+int e2d_compute_dt(e2d_run* h, int useU, void* dt);
+
+/* make_boundaries (serial_ref/m_run.f90:561-648; cuf make_boundaries_gpu
+ * cuf/m_HydroRun_gpu.cuf:1041-1130) on u (which=0) or u2 (which=1). */
+int e2d_make_boundaries(e2d_run* h, int which);
+
+/* godunov_unsplit (serial_ref/m_run.f90:187-243; cuf/m_HydroRun_gpu.cuf:305-450):
+ * one step from u to u2 (nStep even) or u2 to u (odd) with the given dt, by the
+ * run's implementation version. */
+int e2d_godunov_unsplit(e2d_run* h, int nStep, double dt);
+
+/* The inner loop of serial_ref/main.f90:53-76 for steps nStep0 .. nStep0+nsteps-1,
+ * entirely on the device: dt of each step comes from the running maximum, the
+ * next step's CFL maximum is reduced inside the update kernel, and no host
+ * synchronisation happens between steps (steps are replayed from a captured
+ * CUDA graph).  If dt_log is non-NULL it receives the nsteps dt values
+ * (double or float by precision) and the call synchronises. */
+int e2d_advance(e2d_run* h, int nStep0, int nsteps, void* dt_log);
+
+/* Device time in milliseconds of the last e2d_advance call, measured with CUDA
+ * events recorded on the run's stream around its launches (synchronises). */
+int e2d_last_advance_ms(e2d_run* h, float* ms);
+
+/* Current running maximum of 1/dt (double, whatever the precision). */
+int e2d_get_invdt(e2d_run* h, double* invdt);
+
+/* Health flags accumulated by the kernels since the last call (cleared on read). */
+int e2d_get_health(e2d_run* h, unsigned* flags);
+
+/* Human-readable text of the last error on this thread. */
+const char* e2d_last_error(void);
+
+/* Device pointers to u / u2 (pitched SoA planes) for in-process callers that
+ * keep the state resident, with the row pitch in elements and plane stride. */
+int e2d_device_state(e2d_run* h, int which, void** dptr, size_t* pitch_elems,
+                     size_t* plane_elems);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
