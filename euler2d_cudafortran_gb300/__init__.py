@@ -47,7 +47,7 @@ EXPORTED_SYMBOLS = [
     "e2d_default_params", "e2d_create", "e2d_destroy", "e2d_get_sizes", "e2d_set_stream", "e2d_synchronize",
     "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
-    "e2d_get_health", "e2d_last_error", "e2d_device_state",
+    "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
 ]
 
 
@@ -100,6 +100,8 @@ def load_library(path: str = LIB_PATH):
         "e2d_godunov_unsplit": [vp, i, d],
         "e2d_advance": [vp, i, i, vp],
         "e2d_last_advance_ms": [vp, ctypes.POINTER(ctypes.c_float)],
+        "e2d_time_steps": [vp, i, i, ctypes.POINTER(ctypes.c_float)],
+        "e2d_measure_fp64_peak": [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
         "e2d_get_invdt": [vp, ctypes.POINTER(ctypes.c_double)],
         "e2d_get_health": [vp, ctypes.POINTER(ctypes.c_uint)],
         "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
@@ -221,6 +223,13 @@ class HydroRun:
         _check(self._lib.e2d_last_advance_ms(self._h, ctypes.byref(ms)))
         return ms.value
 
+    def time_steps(self, nStep0: int, nsteps: int) -> np.ndarray:
+        """Per-step device time (ms) of nsteps steps launched one by one."""
+        ms = np.zeros(nsteps, dtype=np.float32)
+        _check(self._lib.e2d_time_steps(self._h, nStep0, nsteps,
+                                        ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return ms
+
     def synchronize(self):
         _check(self._lib.e2d_synchronize(self._h))
 
@@ -240,6 +249,13 @@ class HydroRun:
     def final_state(self, nsteps: int) -> np.ndarray:
         """The state after nsteps steps from u: u if nsteps is even, else u2."""
         return self.get_state(nsteps % 2)
+
+
+def measure_fp64_peak():
+    """(independent DFMA/s, IEEE double divisions/s) measured on the current GPU."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(load_library().e2d_measure_fp64_peak(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def run_steps(nsteps: int, params: Params | None = None, u0: np.ndarray | None = None,

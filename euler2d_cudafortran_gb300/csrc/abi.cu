@@ -8,6 +8,7 @@
 #include <map>
 #include <string>
 #include <tuple>
+#include <vector>
 
 #include "../../include/euler2d_gb300.h"
 #include "launch.h"
@@ -55,8 +56,11 @@ struct e2d_run {
   bool timed = false;
   FusedPlan* plan = nullptr;
   int cur_slot = 0;
-  std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
   bool use_graphs = true;
+  // folded[b]: the running CFL maximum (slot cur_slot) already includes the
+  // current state of buffer b (0 = u, 1 = u2), so compute_dt on it needs no sweep.
+  bool folded[2] = {false, false};
 };
 
 namespace {
@@ -159,10 +163,10 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
 // The device work of e2d_advance: compute_dt on the state of nStep0, ghost
 // fill, then nsteps steps with device-resident dt.
 template <typename Real>
-void enqueue_advance(e2d_run* r, int nStep0, int nsteps, int slot0) {
+void enqueue_advance(e2d_run* r, int nStep0, int nsteps, int slot0, bool seed) {
   const Hydro<Real>& h = hydro<Real>(r);
   Field<Real> cur = field<Real>(r, (nStep0 % 2 == 0) ? r->u : r->u2);
-  launch_dt_reduce<Real>(h, cur, r->ctl, slot0, r->stream);
+  if (seed) launch_dt_reduce<Real>(h, cur, r->ctl, slot0, r->stream);
   launch_boundaries<Real>(h, cur, r->stream);
   for (int k = 0; k < nsteps; ++k) {
     const int rd = slot0 ^ (k & 1);
@@ -182,6 +186,22 @@ int finish_dt(e2d_run* r, void* dt_out) {
   E2D_CK(cudaStreamSynchronize(r->stream));
   const Real dt = hydro<Real>(r).cfl / inv;
   *static_cast<Real*>(dt_out) = dt;
+  return E2D_OK;
+}
+
+int ensure_dt_log(e2d_run* r, int nsteps) {
+  if (nsteps <= r->dt_log_cap) return E2D_OK;
+  E2D_CK(cudaStreamSynchronize(r->stream));
+  for (auto& kv : r->graphs) cudaGraphExecDestroy(kv.second);  // they captured the old pointer
+  r->graphs.clear();
+  cudaFree(r->dt_log);
+  r->dt_log = nullptr;
+  r->dt_log_cap = 0;
+  if (cudaMalloc(&r->dt_log, (size_t)nsteps * r->es) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(E2D_ERR_OOM, "cudaMalloc of the dt log failed");
+  }
+  r->dt_log_cap = nsteps;
   return E2D_OK;
 }
 
@@ -327,6 +347,7 @@ int e2d_synchronize(e2d_run* r) {
 int e2d_init_diagonal(e2d_run* r, double offset, double rho_hi, double p_hi, double rho_lo, double p_lo) {
   if (int rc = check_run(r)) return rc;
   if (int rc = use_device(r)) return rc;
+  r->folded[0] = false;
   if (r->es == 8)
     launch_init_diagonal<double>(r->hd, field<double>(r, r->u), offset, rho_hi, p_hi, rho_lo, p_lo, r->stream);
   else
@@ -347,6 +368,7 @@ int e2d_upload_state(e2d_run* r, int which, const void* host) {
   if (!host || (which != 0 && which != 1)) return fail(E2D_ERR_INVALID_ARG, "bad upload arguments");
   if (int rc = use_device(r)) return rc;
   const size_t w = (size_t)r->isize * r->es;
+  r->folded[which] = false;
   E2D_CK(cudaMemcpy2DAsync(which ? r->u2 : r->u, r->pitch * r->es, host, w, w, (size_t)4 * r->jsize,
                            cudaMemcpyHostToDevice, r->stream));
   E2D_CK(cudaStreamSynchronize(r->stream));
@@ -368,14 +390,17 @@ int e2d_compute_dt(e2d_run* r, int useU, void* dt) {
   if (int rc = check_run(r)) return rc;
   if (!dt || (useU != 0 && useU != 1)) return fail(E2D_ERR_INVALID_ARG, "bad compute_dt arguments");
   if (int rc = use_device(r)) return rc;
-  if (r->es == 8) {
-    launch_dt_reduce<double>(r->hd, field<double>(r, useU ? r->u2 : r->u), r->ctl, r->cur_slot, r->stream);
+  // The max is idempotent: when the step that wrote this state already folded
+  // its CFL maximum into the running maximum, a second sweep cannot change it.
+  if (!r->folded[useU]) {
+    if (r->es == 8)
+      launch_dt_reduce<double>(r->hd, field<double>(r, useU ? r->u2 : r->u), r->ctl, r->cur_slot, r->stream);
+    else
+      launch_dt_reduce<float>(r->hf, field<float>(r, useU ? r->u2 : r->u), r->ctl, r->cur_slot, r->stream);
     E2D_CK(cudaGetLastError());
-    return finish_dt<double>(r, dt);
+    r->folded[useU] = true;
   }
-  launch_dt_reduce<float>(r->hf, field<float>(r, useU ? r->u2 : r->u), r->ctl, r->cur_slot, r->stream);
-  E2D_CK(cudaGetLastError());
-  return finish_dt<float>(r, dt);
+  return r->es == 8 ? finish_dt<double>(r, dt) : finish_dt<float>(r, dt);
 }
 
 int e2d_make_boundaries(e2d_run* r, int which) {
@@ -392,9 +417,12 @@ int e2d_godunov_unsplit(e2d_run* r, int nStep, double dt) {
   if (int rc = check_run(r)) return rc;
   if (nStep < 0) return fail(E2D_ERR_INVALID_ARG, "nStep must be >= 0");
   if (int rc = use_device(r)) return rc;
-  if (r->es == 8) enqueue_step<double>(r, nStep, dt, false, 0, -1, 0, false);
-  else enqueue_step<float>(r, nStep, (float)dt, false, 0, -1, 0, false);
+  // dt comes from the caller; the update epilogue folds the CFL maximum of
+  // the new state into the running maximum, which the next compute_dt reads.
+  if (r->es == 8) enqueue_step<double>(r, nStep, dt, false, -1, r->cur_slot, 0, false);
+  else enqueue_step<float>(r, nStep, (float)dt, false, -1, r->cur_slot, 0, false);
   E2D_CK(cudaGetLastError());
+  r->folded[(nStep % 2 == 0) ? 1 : 0] = true;
   return E2D_OK;
 }
 
@@ -403,35 +431,22 @@ int e2d_advance(e2d_run* r, int nStep0, int nsteps, void* dt_log) {
   if (nStep0 < 0 || nsteps < 0) return fail(E2D_ERR_INVALID_ARG, "nStep0 and nsteps must be >= 0");
   if (int rc = use_device(r)) return rc;
   if (nsteps == 0) return E2D_OK;
-  if (nsteps > r->dt_log_cap) {
-    E2D_CK(cudaStreamSynchronize(r->stream));
-    for (auto& kv : r->graphs) cudaGraphExecDestroy(kv.second);
-    r->graphs.clear();
-    cudaFree(r->dt_log);
-    r->dt_log = nullptr;
-    r->dt_log_cap = 0;
-    if (cudaMalloc(&r->dt_log, (size_t)nsteps * r->es) != cudaSuccess) {
-      cudaGetLastError();
-      return fail(E2D_ERR_OOM, "cudaMalloc of the dt log failed");
-    }
-    r->dt_log_cap = nsteps;
-  }
+  if (int rc = ensure_dt_log(r, nsteps)) return rc;
   const int slot0 = r->cur_slot;
+  const int b0 = nStep0 % 2;
+  const bool seed = !r->folded[b0];
   auto enqueue = [&]() {
-    if (r->es == 8) enqueue_advance<double>(r, nStep0, nsteps, slot0);
-    else enqueue_advance<float>(r, nStep0, nsteps, slot0);
+    if (r->es == 8) enqueue_advance<double>(r, nStep0, nsteps, slot0, seed);
+    else enqueue_advance<float>(r, nStep0, nsteps, slot0, seed);
   };
-  bool launched = false;
-  E2D_CK(cudaEventRecord(r->ev0, r->stream));
+  cudaGraphExec_t exec = nullptr;
   if (r->use_graphs && r->stream != nullptr) {
-    const auto key = std::make_tuple(nStep0 % 2, slot0, nsteps);
+    const auto key = std::make_tuple(b0, slot0, nsteps, seed ? 1 : 0);
     auto it = r->graphs.find(key);
-    cudaGraphExec_t exec = nullptr;
     if (it != r->graphs.end()) {
       exec = it->second;
     } else {
       cudaGraph_t graph = nullptr;
-      // ev0 was recorded before capture began, so the capture holds launches only.
       if (cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
         enqueue();
         if (cudaStreamEndCapture(r->stream, &graph) == cudaSuccess && graph) {
@@ -440,20 +455,24 @@ int e2d_advance(e2d_run* r, int nStep0, int nsteps, void* dt_log) {
         }
       }
       cudaGetLastError();
-      if (exec) r->graphs[key] = exec;
-    }
-    if (exec) {
-      E2D_CK(cudaGraphLaunch(exec, r->stream));
-      launched = true;
+      if (exec) {
+        cudaGraphUpload(exec, r->stream);
+        r->graphs[key] = exec;
+      }
     }
   }
-  if (!launched) {
+  // Capture and instantiation happen before ev0, so the events bracket device work only.
+  E2D_CK(cudaEventRecord(r->ev0, r->stream));
+  if (exec) {
+    E2D_CK(cudaGraphLaunch(exec, r->stream));
+  } else {
     enqueue();
     E2D_CK(cudaGetLastError());
   }
   E2D_CK(cudaEventRecord(r->ev1, r->stream));
   r->timed = true;
   r->cur_slot = slot0 ^ (nsteps & 1);
+  r->folded[0] = r->folded[1] = true;
   if (dt_log) {
     E2D_CK(cudaMemcpyAsync(dt_log, r->dt_log, (size_t)nsteps * r->es, cudaMemcpyDeviceToHost, r->stream));
     E2D_CK(cudaStreamSynchronize(r->stream));
@@ -461,6 +480,41 @@ int e2d_advance(e2d_run* r, int nStep0, int nsteps, void* dt_log) {
     E2D_CK(cudaMemcpy(&health, &r->ctl->health, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (health & E2D_HEALTH_DT_NONFINITE) return fail(E2D_ERR_NUMERICS, "dt became non-finite");
   }
+  return E2D_OK;
+}
+
+int e2d_time_steps(e2d_run* r, int nStep0, int nsteps, float* ms) {
+  if (int rc = check_run(r)) return rc;
+  if (nStep0 < 0 || nsteps <= 0 || !ms) return fail(E2D_ERR_INVALID_ARG, "bad time_steps arguments");
+  if (int rc = use_device(r)) return rc;
+  if (int rc = ensure_dt_log(r, nsteps)) return rc;
+  std::vector<cudaEvent_t> ev(nsteps + 1, nullptr);
+  for (auto& e : ev) E2D_CK(cudaEventCreate(&e));
+  const int slot0 = r->cur_slot;
+  const bool seed = !r->folded[nStep0 % 2];
+  const bool v0 = r->p.implementation_version == 0;
+  if (r->es == 8) {
+    Field<double> cur = field<double>(r, (nStep0 % 2 == 0) ? r->u : r->u2);
+    if (seed) launch_dt_reduce<double>(r->hd, cur, r->ctl, slot0, r->stream);
+    launch_boundaries<double>(r->hd, cur, r->stream);
+  } else {
+    Field<float> cur = field<float>(r, (nStep0 % 2 == 0) ? r->u : r->u2);
+    if (seed) launch_dt_reduce<float>(r->hf, cur, r->ctl, slot0, r->stream);
+    launch_boundaries<float>(r->hf, cur, r->stream);
+  }
+  cudaEventRecord(ev[0], r->stream);
+  for (int k = 0; k < nsteps; ++k) {
+    const int rd = slot0 ^ (k & 1);
+    if (r->es == 8) enqueue_step<double>(r, nStep0 + k, 0.0, true, rd, rd ^ 1, k, v0 || k == 0);
+    else enqueue_step<float>(r, nStep0 + k, 0.0f, true, rd, rd ^ 1, k, v0 || k == 0);
+    cudaEventRecord(ev[k + 1], r->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(r->stream);
+  for (int k = 0; k < nsteps && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(e, "e2d_time_steps");
+  r->cur_slot = slot0 ^ (nsteps & 1);
+  r->folded[0] = r->folded[1] = true;
   return E2D_OK;
 }
 
@@ -500,6 +554,7 @@ int e2d_device_state(e2d_run* r, int which, void** dptr, size_t* pitch_elems, si
   if (int rc = check_run(r)) return rc;
   if (which != 0 && which != 1) return fail(E2D_ERR_INVALID_ARG, "which must be 0 or 1");
   if (dptr) *dptr = which ? r->u2 : r->u;
+  r->folded[0] = r->folded[1] = false;  // the caller may write the state directly
   if (pitch_elems) *pitch_elems = r->pitch;
   if (plane_elems) *plane_elems = r->plane;
   return E2D_OK;

@@ -273,7 +273,10 @@ __global__ void __launch_bounds__(NT, Tile<Real>::MINB)
       m = (tid < NT / 32) ? red[tid] : Real(0);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-      if (tid == 0) atomic_max_slot<Real>(ctl, sd.wr_slot, fmax(m, *inv_slot<Real>(ctl, sd.rd_slot)));
+      if (tid == 0) {
+        if (sd.rd_slot >= 0) m = fmax(m, *inv_slot<Real>(ctl, sd.rd_slot));
+        atomic_max_slot<Real>(ctl, sd.wr_slot, m);
+      }
     }
   }
 }

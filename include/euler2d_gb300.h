@@ -80,7 +80,8 @@ int e2d_destroy(e2d_run* h);
 /* Sizes of the run: isize, jsize and bytes of one host state array. */
 int e2d_get_sizes(const e2d_run* h, int* isize, int* jsize, size_t* state_bytes);
 
-/* Issue all later device work on `stream` (a cudaStream_t; NULL = legacy default). */
+/* Issue all later device work on `stream` (a cudaStream_t); NULL selects the
+ * run's own non-blocking stream (the default). */
 int e2d_set_stream(e2d_run* h, void* stream);
 int e2d_synchronize(e2d_run* h);
 
@@ -121,6 +122,17 @@ int e2d_advance(e2d_run* h, int nStep0, int nsteps, void* dt_log);
 /* Device time in milliseconds of the last e2d_advance call, measured with CUDA
  * events recorded on the run's stream around its launches (synchronises). */
 int e2d_last_advance_ms(e2d_run* h, float* ms);
+
+/* The same device work as e2d_advance(nStep0, nsteps), launched step by step
+ * without a graph, with CUDA events on the run's stream around the device work
+ * of each step; ms[k] receives the time of step k (synchronises).  Used to
+ * time the step kernel for the roofline. */
+int e2d_time_steps(e2d_run* h, int nStep0, int nsteps, float* ms);
+
+/* Measures this GPU's FP64 throughput (independent DFMA per second and IEEE
+ * double divisions per second) on the current device: the roof that binds
+ * the FP64 step.  Not part of the reference; used by the benchmark. */
+int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
 
 /* Current running maximum of 1/dt (double, whatever the precision). */
 int e2d_get_invdt(e2d_run* h, double* invdt);
