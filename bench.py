@@ -1,0 +1,394 @@
+#!/usr/bin/env python
+"""Benchmark of the Euler-2D explicit step on one GB300.
+
+Headline workload: 2048 x 2048 cells, FP64, HLLC flux, MC slopes, reflective
+walls, gamma 1.4, CFL 0.8, diagonal-discontinuity initial state,
+implementationVersion 0 (fused), 100 steps.  A "step" is one time step of the
+reference's HydroRun loop (compute_dt + godunov_unsplit) over the whole grid.
+
+Metric: Mcell-updates/s = nx * ny * steps / time (interior cells; the
+reference's own formula, which counts ghost cells, is reported beside it).
+
+value       device time (CUDA events on the launching stream) of `steps`
+            steps replayed from a CUDA graph, state resident in HBM.
+e2e         wall time of the reference driver's call sequence through the C
+            ABI with host buffers: upload of the initial state from pinned
+            memory, compute_dt (dt read back to the host every step) and
+            godunov_unsplit per step, download of the final state.
+roofline    HBM roofline of the step kernel (64 B per cell update in FP64:
+            read U, write U'), plus the FP64 pipe roof that actually binds it.
+cpu_baseline  the CPU oracle (serial_ref restatement) on a bounded sample.
+
+`--impl reference` times the CPU implementation of the reference's path (the
+oracle port: no Fortran compiler exists on the GPU machine) with all host threads on
+the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL = {8: 64, 4: 32}  # read U (4 words) + write U' (4 words)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nx", type=int, default=2048)
+    ap.add_argument("--precision", type=int, choices=[4, 8], default=8)
+    ap.add_argument("--version", type=int, choices=[0, 1, 2], default=0)
+    ap.add_argument("--riemann", choices=["hllc", "approx"], default="hllc")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the single-thread CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- distributed
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Replicas only: each rank advances its own grid on its own GPU; the
+    process group carries the barrier and the max of the timings, never data."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_info()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+def device_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except ImportError:
+        pass
+
+
+# ---------------------------------------------------------------- clocks
+
+CLOCK_Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={CLOCK_Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        under = [s for s in sm if s > 0.5 * mx] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": under[len(under) // 2], "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+# ---------------------------------------------------------------- helpers
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(precision: int, nx: int, version: int):
+    """dram bytes (read + write) per launch of the step kernel from the committed
+    ncu summary of the same workload, if there is one."""
+    name = f"k_fused_{nx}_{'fp64' if precision == 8 else 'fp32'}_traffic.txt" if version == 0 else None
+    if not name:
+        return None
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def workload_name(a):
+    prec = "FP64" if a.precision == 8 else "FP32"
+    return (f"euler2d {a.nx}x{a.nx} {prec}, {a.riemann.upper()} flux, MC slopes, reflective walls, "
+            f"gamma 1.4, CFL 0.8, diagonal discontinuity, implementationVersion {a.version}")
+
+
+def oracle_params(a):
+    from oracle import oracle as O
+    return O.Params(nx=a.nx, ny=a.nx, gamma0=1.4, cfl=0.8, riemann=2 if a.riemann == "hllc" else 0)
+
+
+def time_oracle(a, nsteps: int, nthreads: int):
+    """Wall time of nsteps oracle steps (after one untimed step)."""
+    from oracle import oracle as O
+    p = oracle_params(a)
+    prec = "f64" if a.precision == 8 else "f32"
+    u = O.init_implode(p, prec)
+    _, _, u, u2 = O.run(p, 1, prec=prec, u0=u, nthreads=nthreads)  # warm-up step: state after 1 step in u2
+    t0 = time.perf_counter()
+    O.run(p, nsteps, prec=prec, u0=u2, nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+# ---------------------------------------------------------------- reference arm
+
+def run_reference(a, dist):
+    if dist.rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    nthreads = os.cpu_count() or 1
+    cells = a.nx * a.nx
+    if a.warmup:
+        time_oracle(a, max(1, min(a.warmup, 2)), nthreads)
+    t = time_oracle(a, a.steps, nthreads)
+    v = cells * a.steps / t / 1e6
+    line = {
+        "impl": "reference", "metric": "Mcell-updates/s", "value": round(v, 3), "unit": "Mcell-updates/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1e3 * t / a.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if a.precision == 8 else "f32", "data": "synthetic",
+        "config": {"workload": workload_name(a), "nx": a.nx, "ny": a.nx},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Mcell-updates/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{a.nx}x{a.nx}, {a.steps} steps: CPU restatement of serial_ref (no Fortran "
+                                   f"compiler on the box) with OpenMP on the do-concurrent loops of stdpar"},
+        "e2e": {"value": round(v, 3), "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm
+
+def run_ours(a, dist):
+    import numpy as np
+    import euler2d_cudafortran_gb300 as E
+    E.load_library()
+    cells = a.nx * a.nx
+    params = E.make_params(nx=a.nx, ny=a.nx, gamma0=1.4, cfl=0.8, implementation_version=a.version,
+                           riemann_solver=E.RIEMANN_HLLC if a.riemann == "hllc" else E.RIEMANN_APPROX,
+                           precision=a.precision)
+    run = E.HydroRun(params)
+    run.init_implode()
+    # warm-up: W steps (also builds and uploads the graphs)
+    run.advance(0, a.warmup, log=False)
+    run.advance(a.warmup, a.steps, log=False)  # untimed pass that captures the timed graph
+    run.synchronize()
+    n0 = a.warmup + a.steps
+    dist.barrier()
+    device_sync()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    device_sync()
+    run.advance(n0, a.steps, log=False)
+    ms = run.last_advance_ms()
+    device_sync()
+    dist.barrier()
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    value = dist.ws * cells * a.steps / (ms * 1e-3) / 1e6
+    n0 += a.steps
+
+    # step-kernel time for the roofline: steps launched one by one with events
+    per_step = run.time_steps(n0, 10)
+    n0 += 10
+    kern_ms = float(np.mean(per_step[1:]))
+    hbm_peak, peak_kind = measured_peaks()
+    bytes_per_launch = BYTES_PER_CELL[a.precision] * cells
+    achieved = bytes_per_launch / (kern_ms * 1e-3) / 1e9
+    traffic = profiled_traffic(a.precision, a.nx, a.version)
+    dfma, ddiv = E.measure_fp64_peak()
+    health = run.health()
+    run.close()
+
+    # e2e through the C ABI with host buffers, as serial_ref/main.f90 drives the path
+    e2e = None
+    if not a.no_e2e:
+        try:
+            import torch
+            host_u = torch.empty((4, a.nx + 4, a.nx + 4), dtype=torch.float64 if a.precision == 8 else torch.float32,
+                                 pin_memory=True).numpy()
+            host_out = torch.empty_like(torch.from_numpy(host_u)).pin_memory().numpy()
+        except Exception:
+            host_u = np.empty((4, a.nx + 4, a.nx + 4), dtype=np.float64 if a.precision == 8 else np.float32)
+            host_out = np.empty_like(host_u)
+        with E.HydroRun(params) as r2:
+            r2.init_implode()
+            host_u[...] = r2.get_state(0)
+        with E.HydroRun(params) as r2:
+            # one untimed pass of the same sequence (graph-free path, kernels loaded)
+            for rep in range(2):
+                dist.barrier()
+                device_sync()
+                t0 = time.perf_counter()
+                r2.set_state(0, host_u)
+                r2.compute_dt(0)
+                r2.make_boundaries(0)
+                for n in range(a.steps):
+                    dt = r2.compute_dt(n % 2)
+                    r2.godunov_unsplit(n, dt)
+                host_out[...] = r2.get_state(a.steps % 2)
+                device_sync()
+                t = time.perf_counter() - t0
+            t = dist.max(t)
+        sb = host_u.nbytes
+        e2e = {"value": round(dist.ws * cells * a.steps / t / 1e6, 3), "unit": "Mcell-updates/s",
+               "h2d_bytes_per_step": round(sb / a.steps, 1),
+               "d2h_bytes_per_step": round((sb + a.precision * a.steps) / a.steps, 1),
+               "sequence": "upload u (pinned) -> per step compute_dt (dt read back) + godunov_unsplit -> "
+                           "download final state"}
+
+    # CPU baseline: single-thread restatement of serial_ref on a bounded sample
+    cpu = None
+    cpu_mc = None
+    if dist.rank == 0 and not a.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        t = time_oracle(a, a.cpu_steps, 1)
+        cpu = {"value": round(cells * a.cpu_steps / t / 1e6, 3), "unit": "Mcell-updates/s", "cores": 1,
+               "kind": "port", "sample": f"{a.nx}x{a.nx}, {a.cpu_steps} steps after 1 warm-up step, single thread: "
+                                         "C restatement of serial_ref (-O2 -ffp-contract=off)"}
+        nt = os.cpu_count() or 1
+        steps_mc = 10
+        t = time_oracle(a, steps_mc, nt)
+        cpu_mc = {"value": round(cells * steps_mc / t / 1e6, 3), "unit": "Mcell-updates/s", "cores": nt,
+                  "kind": "port", "sample": f"{a.nx}x{a.nx}, {steps_mc} steps, OpenMP on the stdpar do-concurrent "
+                                            "loops (stand-in for the unavailable -stdpar=multicore build)"}
+
+    variants = None
+    if dist.rank == 0 and not a.no_variants:
+        variants = []
+        for (nx, prec, ver) in ((2048, 8, 1), (2048, 4, 0), (2048, 4, 1), (4096, 8, 0), (4096, 4, 0)):
+            p = E.make_params(nx=nx, ny=nx, gamma0=1.4, cfl=0.8, implementation_version=ver,
+                              riemann_solver=params.riemann_solver, precision=prec)
+            with E.HydroRun(p) as r3:
+                r3.init_implode()
+                ns = 20
+                r3.advance(0, 3, log=False)
+                r3.advance(3, ns, log=False)
+                r3.advance(3 + ns, ns, log=False)
+                vms = r3.last_advance_ms()
+            variants.append({"nx": nx, "precision": "FP64" if prec == 8 else "FP32", "implementationVersion": ver,
+                             "steps": ns, "mcells_per_s": round(nx * nx * ns / (vms * 1e-3) / 1e6, 2)})
+
+    if dist.rank == 0:
+        isz = a.nx + 4
+        line = {
+            "metric": "Mcell-updates/s", "value": round(value, 3), "unit": "Mcell-updates/s",
+            "n_gpus": dist.ws, "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms / a.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if a.precision == 8 else "f32", "data": "synthetic",
+            "config": {"workload": workload_name(a), "nx": a.nx, "ny": a.nx, "steps": a.steps,
+                       "parallelism": "replicas" if dist.ws > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (u and u2: 2 x %.1f MB ping-pong per step)"
+                             % (4 * isz * isz * a.precision / 1e6)},
+            "value_reference_formula": round(dist.ws * isz * isz * a.steps / (ms * 1e-3) / 1e6, 3),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(achieved / hbm_peak, 5), "peak_kind": peak_kind,
+                         "traffic": traffic,
+                         "bytes_per_launch": bytes_per_launch, "kernel_ms": round(kern_ms, 4),
+                         "binding_roof": {"pipe": "fp64", "dfma_per_s": dfma, "ddiv_per_s": ddiv,
+                                          "note": "the FP64 step is bound by the FP64 pipe (divisions and "
+                                                  "square roots of two Riemann solves per cell), not by HBM"}},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "cpu_baseline_multicore": cpu_mc,
+            "clocks": clk,
+            "gpu_launches": a.steps + 1 if a.version == 0 else 4 * a.steps,
+            "health_flags": health,
+            "variants": variants,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse_args()
+    ws, rank, local = dist_info()
+    if ws > 1:
+        # one GPU per rank, visible to both this process's CUDA runtimes
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = Dist()
+    try:
+        if a.impl == "reference":
+            run_reference(a, dist)
+        else:
+            run_ours(a, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -41,7 +41,7 @@ class RunConfig:
     boundary_type_xmax: int = 1
     boundary_type_ymin: int = 1
     boundary_type_ymax: int = 1
-    gamma0: float = 1.4
+    gamma0: float = 1.666
     cfl: float = 0.8
     smallr: float = 1e-7
     smallc: float = 1e-7
