@@ -48,6 +48,7 @@ EXPORTED_SYMBOLS = [
     "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
     "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
+    "e2d_godunov_unsplit_noalloc",
 ]
 
 
@@ -106,6 +107,7 @@ def load_library(path: str = LIB_PATH):
         "e2d_get_health": [vp, ctypes.POINTER(ctypes.c_uint)],
         "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
                              ctypes.POINTER(ctypes.c_size_t)],
+        "e2d_godunov_unsplit_noalloc": [ctypes.POINTER(Params), vp, vp, ctypes.c_size_t, d, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

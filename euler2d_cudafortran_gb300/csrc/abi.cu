@@ -36,6 +36,8 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 }  // namespace
 
+int e2d::set_error(int code, const std::string& msg) { return fail(code, msg); }
+
 struct e2d_run {
   e2d_params p;
   int device = 0;

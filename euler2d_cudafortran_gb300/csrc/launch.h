@@ -1,6 +1,9 @@
 // launch.h -- host-side launchers shared by the translation units of the library.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <string>
+
 #include "physics.cuh"
 
 namespace e2d {
@@ -31,6 +34,10 @@ struct StepDt {
   Real* dt_log;     // device; may be null
   int log_index;
 };
+
+// ---- abi.cu ----
+// Records msg as the text returned by e2d_last_error on this thread; returns code.
+int set_error(int code, const std::string& msg);
 
 // ---- k_sweeps.cu ----
 template <typename Real> void launch_init_diagonal(const Hydro<Real>& h, Field<Real> u, double offset, double rho_hi,

@@ -148,6 +148,25 @@ const char* e2d_last_error(void);
 int e2d_device_state(e2d_run* h, int which, void** dptr, size_t* pitch_elems,
                      size_t* plane_elems);
 
+/* One godunov_unsplit step (the stored-fluxes variant, implementationVersion 2
+ * arithmetic) that allocates no device memory.  No counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc (device arrays owned
+ * by another allocator or memory pool, or a host framework that forbids
+ * allocation on its time-step path).  u_in and u_out are device arrays in the
+ * pitched layout of e2d_device_state (4 planes of ny+4 rows of pitch_elems
+ * elements); make_boundaries is applied to u_in first, as the reference does.
+ * The work arrays live in one static device array of
+ * E2D_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * exit; grids whose three work arrays (primitives and two flux arrays) do not
+ * fit are rejected with E2D_ERR_INVALID_ARG.  All calls share that array:
+ * calls that overlap on the GPU race.  The first call on a device looks up
+ * the array's device address and should come before any stream capture.
+ * Work is issued on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * and not synchronised. */
+#define E2D_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
+int e2d_godunov_unsplit_noalloc(const e2d_params* p, void* u_in, void* u_out, size_t pitch_elems, double dt,
+                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif
