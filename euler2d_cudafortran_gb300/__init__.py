@@ -48,7 +48,7 @@ EXPORTED_SYMBOLS = [
     "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
     "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
-    "e2d_godunov_unsplit_noalloc",
+    "e2d_godunov_unsplit_noalloc", "e2d_selftest_arith",
 ]
 
 
@@ -108,6 +108,9 @@ def load_library(path: str = LIB_PATH):
         "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
                              ctypes.POINTER(ctypes.c_size_t)],
         "e2d_godunov_unsplit_noalloc": [ctypes.POINTER(Params), vp, vp, ctypes.c_size_t, d, vp],
+        "e2d_selftest_arith": [i, i, ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong),
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -258,6 +261,18 @@ def measure_fp64_peak():
     a, b = ctypes.c_double(), ctypes.c_double()
     _check(load_library().e2d_measure_fp64_peak(ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+def selftest_arith(op: int, mode: int, n: int, seed: int = 1, rates: bool = False):
+    """Bitwise check of the integer-pipe division (op 0) / square root (op 1)
+    against the hardware on n inputs; returns (mismatches, first_bad[4], rates)."""
+    bad = ctypes.c_ulonglong()
+    first = (ctypes.c_double * 4)()
+    em, na = ctypes.c_double(), ctypes.c_double()
+    _check(load_library().e2d_selftest_arith(op, mode, n, seed, ctypes.byref(bad), first,
+                                              ctypes.byref(em) if rates else None,
+                                              ctypes.byref(na) if rates else None))
+    return bad.value, list(first), ((em.value, na.value) if rates else None)
 
 
 def run_steps(nsteps: int, params: Params | None = None, u0: np.ndarray | None = None,

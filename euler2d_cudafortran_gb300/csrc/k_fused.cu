@@ -42,7 +42,7 @@ struct Smem {
   static constexpr size_t fx_off = s_off + 4ull * RY * RX;             // [4][TY][TX+1]
   static constexpr size_t fy_off = fx_off + 4ull * TY * (TX + 1);      // [4][TY+1][TX]
   static constexpr size_t n_real = fy_off + 4ull * (TY + 1) * TX;
-  static constexpr size_t bytes = n_real * sizeof(Real) + 128 /*mbarrier + counters*/ + 128 /*align*/;
+  static constexpr size_t bytes = n_real * sizeof(Real) + 256 /*mbarrier, counter, reduction, dt*/ + 128 /*align*/;
   static constexpr uint32_t tma_bytes = 4u * BYs * BXs * sizeof(Real);
 };
 
@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(NT, Tile<Real>::MINB)
   uint64_t* bar = reinterpret_cast<uint64_t*>(base + S::n_real);
   int* face_counter = reinterpret_cast<int*>(bar + 1);
   Real* red = reinterpret_cast<Real*>(bar + 2);  // 8 warps
+  Real* sdt = red + 8;                           // dt, dt/dx, dt/dy of this step
 
   const int tid = threadIdx.x;
   const int i0 = GW + blockIdx.x * TX;  // first interior cell of the tile
@@ -113,6 +114,12 @@ __global__ void __launch_bounds__(NT, Tile<Real>::MINB)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     *face_counter = 0;
+    // This step's dt (serial_ref/m_run.f90:308 when it comes from the running
+    // maximum) and dt/dx, dt/dy (m_run.f90:384-385), once per CTA.
+    const Real dt0 = sd.from_slot ? h.cfl / *inv_slot<Real>(ctl, sd.rd_slot) : sd.dt_value;
+    sdt[0] = dt0;
+    sdt[1] = dt0 / h.dx;
+    sdt[2] = dt0 / h.dy;
   }
   __syncthreads();
   if (tid == 0) {
@@ -124,10 +131,9 @@ __global__ void __launch_bounds__(NT, Tile<Real>::MINB)
         "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
         : "memory");
   }
-  // Resolve this step's dt while the tile is in flight.
-  const Real dt = sd.from_slot ? h.cfl / *inv_slot<Real>(ctl, sd.rd_slot) : sd.dt_value;
-  const Real dtdx = dt / h.dx;
-  const Real dtdy = dt / h.dy;
+  const Real dt = sdt[0];
+  const Real dtdx = sdt[1];
+  const Real dtdy = sdt[2];
   const bool ok = mbar_wait(bar_a, 0);
   if (__syncthreads_or(!ok)) {
     if (tid == 0) atomicOr(&ctl->health, 4u);

@@ -1,0 +1,146 @@
+// k_selftest.cu -- on-device check of the emulated double division and square
+// root (emul64.cuh) against the hardware operations, bit for bit, plus their
+// throughput.  Exposed as e2d_selftest_arith for the GPU tests.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/euler2d_gb300.h"
+#include "emul64.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {  // splitmix64 finaliser
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// Random double: mode 0 any finite/special bit pattern, mode 1 exponent within
+// +-40 of 1, mode 2 exponent within +-400 of 1.
+__device__ double rand_double(uint64_t r, int mode) {
+  if (mode == 0) return __longlong_as_double((long long)r);
+  const int span = mode == 1 ? 40 : 400;
+  const uint64_t e = (uint64_t)(1023 - span + (int)((r >> 52) % (uint64_t)(2 * span + 1)));
+  return __longlong_as_double((long long)((r & 0x800fffffffffffffull) | (e << 52)));
+}
+
+__device__ bool same(double x, double y) {
+  const uint64_t a = (uint64_t)__double_as_longlong(x), b = (uint64_t)__double_as_longlong(y);
+  if (x != x && y != y) return true;  // both NaN
+  return a == b;
+}
+
+// op 0: division, op 1: square root.  Modes 0-2 as rand_double; mode 4 signed
+// zeros and small integers; mode 3 builds
+// operands whose exact result lies within one part in 2^60 of a rounding
+// boundary (quotient q + 1/2 ulp times b, or (q + 1/2 ulp)^2).
+__global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned long long* bad, double* first) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const uint64_t r1 = mix64(seed ^ (uint64_t)k), r2 = mix64(r1 + 0x1234567ull);
+    double a, b = 1.0;
+    if (mode < 3) {
+      a = rand_double(r1, mode);
+      b = rand_double(r2, mode);
+    } else if (mode == 4) {  // signed zeros and small integers over random denominators
+      a = (r1 & 4) ? 0.0 : (double)(int)((r1 >> 8) & 7);
+      a = (r1 & 1) ? -a : a;
+      b = rand_double(r2, (r2 & 1) ? 0 : 2);
+      if (op == 1) a = (r1 & 4) ? a : (double)((r1 >> 8) & 7);
+    } else if (op == 0) {
+      b = rand_double(r2, 1);
+      const double q = rand_double(r1, 1);
+      const double qm = q + 0.5 * (__longlong_as_double(__double_as_longlong(q) + 1) - q);  // rounds to a neighbour
+      a = __dmul_rn(qm, b);
+      a = __longlong_as_double(__double_as_longlong(a) + (long long)(r1 & 3) - 1);
+    } else {
+      const double q = fabs(rand_double(r1, 1));
+      const double h = 0.5 * (__longlong_as_double(__double_as_longlong(q) + 1) - q);
+      a = __dmul_rn(q + h, q + h);
+      a = __longlong_as_double(__double_as_longlong(a) + (long long)(r2 & 3) - 1);
+    }
+    const double x = op == 0 ? e2d::emul::div_rn(a, b) : e2d::emul::sqrt_rn(a);
+    const double y = op == 0 ? __ddiv_rn(a, b) : __dsqrt_rn(a);
+    if (!same(x, y)) {
+      if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
+    }
+  }
+}
+
+__global__ void k_rate(int op, int emulated, int iters, double* out) {
+  double x0 = 1.0 + threadIdx.x * 1e-3, x1 = x0 + 0.25, x2 = x0 + 0.5, x3 = x0 + 0.75;
+  const double c = 0.999;
+  for (int i = 0; i < iters; ++i) {
+    if (op == 0) {
+      if (emulated) {
+        x0 = e2d::emul::div_rn(c, x0) + 1.0; x1 = e2d::emul::div_rn(c, x1) + 1.0;
+        x2 = e2d::emul::div_rn(c, x2) + 1.0; x3 = e2d::emul::div_rn(c, x3) + 1.0;
+      } else {
+        x0 = c / x0 + 1.0; x1 = c / x1 + 1.0; x2 = c / x2 + 1.0; x3 = c / x3 + 1.0;
+      }
+    } else {
+      if (emulated) {
+        x0 = e2d::emul::sqrt_rn(x0) + 1.0; x1 = e2d::emul::sqrt_rn(x1) + 1.0;
+        x2 = e2d::emul::sqrt_rn(x2) + 1.0; x3 = e2d::emul::sqrt_rn(x3) + 1.0;
+      } else {
+        x0 = sqrt(x0) + 1.0; x1 = sqrt(x1) + 1.0; x2 = sqrt(x2) + 1.0; x3 = sqrt(x3) + 1.0;
+      }
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
+}
+
+}  // namespace
+
+extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
+                                  unsigned long long* mismatches, double* first_bad, double* emulated_per_s,
+                                  double* native_per_s) {
+  if ((op != 0 && op != 1) || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return E2D_ERR_NO_DEVICE;
+  }
+  unsigned long long* d_bad = nullptr;
+  double* d_first = nullptr;
+  double* d_out = nullptr;
+  const int threads = 256, blocks = sms * 8;
+  if (cudaMalloc(&d_bad, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&d_first, 4 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_out, (size_t)threads * blocks * sizeof(double)) != cudaSuccess) {
+    cudaFree(d_bad);
+    cudaFree(d_first);
+    cudaGetLastError();
+    return E2D_ERR_OOM;
+  }
+  cudaMemset(d_bad, 0, sizeof(unsigned long long));
+  cudaMemset(d_first, 0, 4 * sizeof(double));
+  k_check<<<blocks, threads>>>(op, mode, n, seed, d_bad, d_first);
+  cudaMemcpy(mismatches, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (first_bad) cudaMemcpy(first_bad, d_first, 4 * sizeof(double), cudaMemcpyDeviceToHost);
+  if (emulated_per_s && native_per_s) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int iters = 400;
+    for (int emulated = 0; emulated < 2; ++emulated) {
+      k_rate<<<blocks, threads>>>(op, emulated, 8, d_out);
+      cudaEventRecord(e0);
+      k_rate<<<blocks, threads>>>(op, emulated, iters, d_out);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const double rate = (double)threads * blocks * iters * 4 / (ms * 1e-3);
+      *(emulated ? emulated_per_s : native_per_s) = rate;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  const cudaError_t e = cudaDeviceSynchronize();
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  cudaFree(d_out);
+  return e == cudaSuccess ? E2D_OK : E2D_ERR_CUDA;
+}

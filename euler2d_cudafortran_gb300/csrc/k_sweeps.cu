@@ -16,7 +16,7 @@ inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) /
 
 template <typename Real>
 __device__ __forceinline__ Real resolve_dt(const Hydro<Real>& h, const StepDt<Real>& sd, Ctl* ctl) {
-  if (sd.from_slot) return h.cfl / *inv_slot<Real>(ctl, sd.rd_slot);
+  if (sd.from_slot) return Ops<Real>::div(h.cfl, *inv_slot<Real>(ctl, sd.rd_slot));
   return sd.dt_value;
 }
 
@@ -163,8 +163,8 @@ __global__ void k_fluxes_v2(Hydro<Real> h, Field<Real> q, StepDt<Real> sd, Ctl* 
   const int j = GW + blockIdx.y * blockDim.y + threadIdx.y;
   if (i > h.isize - 2 || j > h.jsize - 2) return;
   const Real dt = resolve_dt(h, sd, ctl);
-  const Real dtdx = dt / h.dx;
-  const Real dtdy = dt / h.dy;
+  const Real dtdx = Ops<Real>::div(dt, h.dx);
+  const Real dtdy = Ops<Real>::div(dt, h.dy);
   Real qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4];
   Real qN[4], qNe[4], qNw[4], qNn[4], qNs[4], dqNx[4], dqNy[4], sN[4];
   Real qleft[4], qright[4], flux[4];
@@ -245,8 +245,8 @@ __global__ void k_trace_v1(Hydro<Real> h, Field<Real> q, StepDt<Real> sd, Ctl* c
   const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (i > h.isize - 2 || j > h.jsize - 2) return;
   const Real dt = resolve_dt(h, sd, ctl);
-  const Real dtdx = dt / h.dx;
-  const Real dtdy = dt / h.dy;
+  const Real dtdx = Ops<Real>::div(dt, h.dx);
+  const Real dtdy = Ops<Real>::div(dt, h.dy);
   Real qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4], f[4];
   load4(q, j, i, qc); load4(q, j, i + 1, qe); load4(q, j, i - 1, qw); load4(q, j + 1, i, qn); load4(q, j - 1, i, qs);
   slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
@@ -270,8 +270,8 @@ __global__ void __launch_bounds__(BX * BY) k_flux_update_v1(Hydro<Real> h, Field
   const int tid = threadIdx.x + threadIdx.y * BX;
   const int i0 = GW + blockIdx.x * TX, j0 = GW + blockIdx.y * TY;
   const Real dt = resolve_dt(h, sd, ctl);
-  const Real dtdx = dt / h.dx;
-  const Real dtdy = dt / h.dy;
+  const Real dtdx = Ops<Real>::div(dt, h.dx);
+  const Real dtdy = Ops<Real>::div(dt, h.dy);
   // x-faces: face f (0..TX) of row r sits between cells i0+f-1 and i0+f
   for (int k = tid; k < (TX + 1) * TY; k += BX * BY) {
     const int f = k % (TX + 1), r = k / (TX + 1);

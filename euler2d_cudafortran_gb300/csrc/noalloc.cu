@@ -26,6 +26,7 @@
 #include <string>
 
 #include "../../include/euler2d_gb300.h"
+#include "hydro_params.h"
 #include "launch.h"
 
 using namespace e2d;
@@ -67,37 +68,9 @@ int scratch_address(void** out) {
 }
 
 template <typename Real>
-Hydro<Real> hydro_of(const e2d_params& p) {
-  // Same derived parameters as a run handle (serial_ref/m_run.f90:95-124).
-  Hydro<Real> h;
-  const Real xmin = Real(0.0), xmax = Real(1.0);
-  h.nx = p.nx;
-  h.ny = p.ny;
-  h.isize = p.nx + 4;
-  h.jsize = p.ny + 4;
-  h.dx = (xmax - xmin) / (Real)p.nx;
-  h.dy = (xmax - xmin) / (Real)p.ny;
-  h.gamma0 = (Real)p.gamma0;
-  h.cfl = (Real)p.cfl;
-  h.smallr = (Real)p.smallr;
-  h.smallc = (Real)p.smallc;
-  h.niter_riemann = p.niter_riemann;
-  h.slope_type = p.slope_type;
-  h.smallp = h.smallc * h.smallc / h.gamma0;
-  h.smallpp = h.smallr * h.smallp;
-  h.gamma6 = (h.gamma0 + Real(1.0)) / (Real(2.0) * h.gamma0);
-  h.bc_xmin = p.boundary_type_xmin;
-  h.bc_xmax = p.boundary_type_xmax;
-  h.bc_ymin = p.boundary_type_ymin;
-  h.bc_ymax = p.boundary_type_ymax;
-  h.riemann = p.riemann_solver;
-  return h;
-}
-
-template <typename Real>
 int step(const e2d_params& p, void* u_in, void* u_out, size_t pitch, double dt, unsigned char* scratch,
          size_t work_pitch, cudaStream_t s) {
-  const Hydro<Real> h = hydro_of<Real>(p);
+  const Hydro<Real> h = make_hydro<Real>(p);
   const long long plane = (long long)pitch * h.jsize;
   const long long wplane = (long long)work_pitch * h.jsize;
   Field<Real> in{static_cast<Real*>(u_in), (int)pitch, plane};

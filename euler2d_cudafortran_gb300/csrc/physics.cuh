@@ -11,9 +11,18 @@
 // default-real literals stay single precision in both builds:
 //   1e-6 (Newton tolerance, serial_ref/m_utils.f90:396) and 0.14
 //   (init_implode, serial_ref/m_run.f90:548).
+//
+// Every division, square root, comparison, min/max, multiplication by 0.5 or
+// 2 and sign flip goes through Ops<Real>.  For double these run on the
+// integer and FP32 pipes (emul64.cuh) and return the same bits as the IEEE
+// operations, which leaves the FP64 pipe -- the limit of this kernel on
+// GB300 -- to the additions and multiplications.  Building with
+// -DE2D_FP64_NATIVE selects the hardware FP64 operations instead.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "emul64.cuh"
 
 namespace e2d {
 
@@ -21,13 +30,73 @@ enum { ID = 0, IP = 1, IU = 2, IV = 3 };  // serial_ref/m_constants.f90:11-14, 0
 enum { FACE_XMIN = 0, FACE_XMAX = 1, FACE_YMIN = 2, FACE_YMAX = 3 };
 constexpr int GW = 2;  // ghostWidth, serial_ref/m_run.f90:28
 
-// type HydroPar (serial_ref/m_parameters.f90:10-36) in the working precision.
+// type HydroPar (serial_ref/m_parameters.f90:10-36) in the working precision,
+// plus three loop-invariant subexpressions of the reference evaluated once on
+// the host with the same operations: gm1 = gamma0 - 1.0 (eos), entho =
+// 1.0 / (gamma0 - 1.0) (cmpflx, riemann_2d_hllc), smallc2 = smallc * smallc.
 template <typename Real>
 struct Hydro {
   Real gamma0, gamma6, cfl, smallr, smallc, smallp, smallpp, dx, dy;
+  Real gm1, entho, smallc2;
   int slope_type, niter_riemann, nx, ny, isize, jsize;
   int bc_xmin, bc_xmax, bc_ymin, bc_ymax, riemann;
 };
+
+template <typename Real> struct Ops;
+
+// FP32: the hardware operations (the FP32 pipes are not the limit).
+template <>
+struct Ops<float> {
+  static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+  static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
+  static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
+  static __device__ __forceinline__ float min(float a, float b) { return fminf(a, b); }
+  static __device__ __forceinline__ bool gt0(float x) { return x > 0.0f; }
+  static __device__ __forceinline__ bool ge0(float x) { return x >= 0.0f; }
+  static __device__ __forceinline__ bool lt0(float x) { return x < 0.0f; }
+  static __device__ __forceinline__ bool le0(float x) { return x <= 0.0f; }
+  static __device__ __forceinline__ bool gt(float a, float b) { return a > b; }
+  static __device__ __forceinline__ bool ge(float a, float b) { return a >= b; }
+  static __device__ __forceinline__ float half(float x) { return 0.5f * x; }
+  static __device__ __forceinline__ float twice(float x) { return 2.0f * x; }
+  static __device__ __forceinline__ float neg_if(float x, bool n) { return n ? -x : x; }
+};
+
+#ifdef E2D_FP64_NATIVE
+template <>
+struct Ops<double> {
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  static __device__ __forceinline__ double sqrt(double a) { return ::sqrt(a); }
+  static __device__ __forceinline__ double max(double a, double b) { return fmax(a, b); }
+  static __device__ __forceinline__ double min(double a, double b) { return fmin(a, b); }
+  static __device__ __forceinline__ bool gt0(double x) { return x > 0.0; }
+  static __device__ __forceinline__ bool ge0(double x) { return x >= 0.0; }
+  static __device__ __forceinline__ bool lt0(double x) { return x < 0.0; }
+  static __device__ __forceinline__ bool le0(double x) { return x <= 0.0; }
+  static __device__ __forceinline__ bool gt(double a, double b) { return a > b; }
+  static __device__ __forceinline__ bool ge(double a, double b) { return a >= b; }
+  static __device__ __forceinline__ double half(double x) { return 0.5 * x; }
+  static __device__ __forceinline__ double twice(double x) { return 2.0 * x; }
+  static __device__ __forceinline__ double neg_if(double x, bool n) { return n ? -x : x; }
+};
+#else
+template <>
+struct Ops<double> {
+  static __device__ __forceinline__ double div(double a, double b) { return emul::div_rn(a, b); }
+  static __device__ __forceinline__ double sqrt(double a) { return emul::sqrt_rn(a); }
+  static __device__ __forceinline__ double max(double a, double b) { return emul::max_i(a, b); }
+  static __device__ __forceinline__ double min(double a, double b) { return emul::min_i(a, b); }
+  static __device__ __forceinline__ bool gt0(double x) { return emul::gt0(x); }
+  static __device__ __forceinline__ bool ge0(double x) { return emul::ge0(x); }
+  static __device__ __forceinline__ bool lt0(double x) { return emul::lt0(x); }
+  static __device__ __forceinline__ bool le0(double x) { return emul::le0(x); }
+  static __device__ __forceinline__ bool gt(double a, double b) { return emul::gt_i(a, b); }
+  static __device__ __forceinline__ bool ge(double a, double b) { return emul::ge_i(a, b); }
+  static __device__ __forceinline__ double half(double x) { return emul::half(x); }
+  static __device__ __forceinline__ double twice(double x) { return emul::twice(x); }
+  static __device__ __forceinline__ double neg_if(double x, bool n) { return emul::neg_if(x, n); }
+};
+#endif
 
 // A pitched structure-of-arrays state: 4 planes of jsize rows of `pitch`
 // elements; element (i, j, v) (0-based) at v*plane + j*pitch + i.
@@ -41,50 +110,55 @@ struct Field {
   }
 };
 
-template <typename Real> __device__ __forceinline__ Real rmax(Real a, Real b) { return fmax(a, b); }
-template <typename Real> __device__ __forceinline__ Real rmin(Real a, Real b) { return fmin(a, b); }
 template <typename Real> __device__ __forceinline__ Real rabs(Real a) { return fabs(a); }
-template <typename Real> __device__ __forceinline__ Real rsqrt_ieee(Real a) { return sqrt(a); }
 
 // eos + computePrimitives, serial_ref/m_utils.f90:15-29 and 35-64, without the
 // sound speed (unused by every caller except compute_dt).
 template <typename Real>
 __device__ __forceinline__ void primitives(const Hydro<Real>& h, const Real u[4], Real q[4]) {
-  q[ID] = rmax(u[ID], h.smallr);
-  q[IU] = u[IU] / q[ID];
-  q[IV] = u[IV] / q[ID];
-  const Real eken = Real(0.5) * ((q[IU] * q[IU]) + (q[IV] * q[IV]));
-  const Real e = (u[IP] / q[ID]) - eken;
-  q[IP] = rmax(((h.gamma0 - Real(1.0)) * q[ID]) * e, q[ID] * h.smallp);
+  using O = Ops<Real>;
+  q[ID] = O::max(u[ID], h.smallr);
+  q[IU] = O::div(u[IU], q[ID]);
+  q[IV] = O::div(u[IV], q[ID]);
+  const Real eken = O::half((q[IU] * q[IU]) + (q[IV] * q[IV]));
+  const Real e = O::div(u[IP], q[ID]) - eken;
+  q[IP] = O::max((h.gm1 * q[ID]) * e, q[ID] * h.smallp);
 }
 
 // Sound speed of eos (serial_ref/m_utils.f90:27) from primitive q.
 template <typename Real>
 __device__ __forceinline__ Real sound_speed(const Hydro<Real>& h, const Real q[4]) {
-  return rsqrt_ieee((h.gamma0 * q[IP]) / q[ID]);
+  using O = Ops<Real>;
+  return O::sqrt(O::div(h.gamma0 * q[IP], q[ID]));
 }
 
 // The compute_dt term of one cell, serial_ref/m_run.f90:278-281.
 template <typename Real>
 __device__ __forceinline__ Real cell_invdt(const Hydro<Real>& h, const Real u[4]) {
+  using O = Ops<Real>;
   Real q[4];
   primitives(h, u, q);
   const Real c = sound_speed(h, q);
   const Real vx = c + rabs(q[IU]);
   const Real vy = c + rabs(q[IV]);
-  return (vx / h.dx) + (vy / h.dy);
+  return O::div(vx, h.dx) + O::div(vy, h.dy);
 }
 
-// One direction of slope_unsplit_hydro_2d, serial_ref/m_utils.f90:300-312.
+// One direction of slope_unsplit_hydro_2d, serial_ref/m_utils.f90:300-312:
+// dlft = st*(q-qm), drgt = st*(qp-q), dcen = 0.5*(qp-qm), dsgn = +-1 by
+// dcen >= 0, dlim = 0 if dlft*drgt <= 0 else min(|dlft|,|drgt|), and the
+// slope dsgn*min(dlim,|dcen|).  st is 1 or 2; the products by st, 0.5 and
+// dsgn are exact scalings and sign flips.
 template <typename Real>
-__device__ __forceinline__ Real slope1(Real st, Real q, Real qp, Real qm) {
-  const Real dlft = st * (q - qm);
-  const Real drgt = st * (qp - q);
-  const Real dcen = Real(0.5) * (qp - qm);
-  const Real dsgn = (dcen >= Real(0.0)) ? Real(1.0) : Real(-1.0);
-  const Real slop = rmin(rabs(dlft), rabs(drgt));
-  const Real dlim = ((dlft * drgt) <= Real(0.0)) ? Real(0.0) : slop;
-  return dsgn * rmin(dlim, rabs(dcen));
+__device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm) {
+  using O = Ops<Real>;
+  const Real dl = q - qm, dr = qp - q;
+  const Real dlft = mc ? O::twice(dl) : dl;
+  const Real drgt = mc ? O::twice(dr) : dr;
+  const Real dcen = O::half(qp - qm);
+  const Real slop = O::min(rabs(dlft), rabs(drgt));
+  const Real dlim = O::le0(dlft * drgt) ? Real(0.0) : slop;
+  return O::neg_if(O::min(dlim, rabs(dcen)), !O::ge0(dcen));
 }
 
 // slope_unsplit_hydro_2d, serial_ref/m_utils.f90:268-342.
@@ -93,11 +167,11 @@ __device__ __forceinline__ void slopes(const Hydro<Real>& h, const Real q[4], co
                                        const Real qmx[4], const Real qpy[4], const Real qmy[4],
                                        Real dqx[4], Real dqy[4]) {
   if (h.slope_type == 1 || h.slope_type == 2) {
-    const Real st = Real(h.slope_type);
+    const bool mc = h.slope_type == 2;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      dqx[v] = slope1(st, q[v], qpx[v], qmx[v]);
-      dqy[v] = slope1(st, q[v], qpy[v], qmy[v]);
+      dqx[v] = slope1(mc, q[v], qpx[v], qmx[v]);
+      dqy[v] = slope1(mc, q[v], qpy[v], qmy[v]);
     }
   } else {
 #pragma unroll
@@ -110,37 +184,39 @@ __device__ __forceinline__ void slopes(const Hydro<Real>& h, const Real q[4], co
 template <typename Real>
 __device__ __forceinline__ void trace_sources(const Hydro<Real>& h, const Real q[4], const Real dqx[4],
                                               const Real dqy[4], Real s[4]) {
+  using O = Ops<Real>;
   const Real r = q[ID], p = q[IP], u = q[IU], v = q[IV];
   s[ID] = ((-(u * dqx[ID])) - (v * dqy[ID])) - ((dqx[IU] + dqy[IV]) * r);
   s[IP] = ((-(u * dqx[IP])) - (v * dqy[IP])) - (((dqx[IU] + dqy[IV]) * h.gamma0) * p);
-  s[IU] = ((-(u * dqx[IU])) - (v * dqy[IU])) - (dqx[IP] / r);
-  s[IV] = ((-(u * dqx[IV])) - (v * dqy[IV])) - (dqy[IP] / r);
+  s[IU] = ((-(u * dqx[IU])) - (v * dqy[IU])) - O::div(dqx[IP], r);
+  s[IV] = ((-(u * dqx[IV])) - (v * dqy[IV])) - O::div(dqy[IP], r);
 }
 
 // Face state of trace_unsplit_2d_along_dir, serial_ref/m_utils.f90:218-252:
 // qf = (q -/+ 0.5*dq_dir) + (s*dtd)*0.5, then rho floored at smallr.
-// sign = -1 for the XMIN/YMIN faces, +1 for XMAX/YMAX; dq is the slope along
-// the face normal, dtd = dtdx or dtdy.
+// PLUS selects the XMAX/YMAX faces; dq is the slope along the face normal,
+// dtd = dtdx or dtdy.
 template <typename Real, bool PLUS>
 __device__ __forceinline__ void trace_face(const Hydro<Real>& h, const Real q[4], const Real dq[4],
                                            const Real s[4], Real dtd, Real qf[4]) {
+  using O = Ops<Real>;
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    const Real a = PLUS ? (q[v] + (Real(0.5) * dq[v])) : (q[v] - (Real(0.5) * dq[v]));
-    qf[v] = a + ((s[v] * dtd) * Real(0.5));
+    const Real a = PLUS ? (q[v] + O::half(dq[v])) : (q[v] - O::half(dq[v]));
+    qf[v] = a + O::half(s[v] * dtd);
   }
-  qf[ID] = rmax(h.smallr, qf[ID]);
+  qf[ID] = O::max(h.smallr, qf[ID]);
 }
 
 // cmpflx, serial_ref/m_utils.f90:498-526.
 template <typename Real>
 __device__ __forceinline__ void cmpflx(const Hydro<Real>& h, const Real qg[4], Real flux[4]) {
+  using O = Ops<Real>;
   flux[ID] = qg[ID] * qg[IU];
   flux[IU] = (flux[ID] * qg[IU]) + qg[IP];
   flux[IV] = flux[ID] * qg[IV];
-  const Real entho = Real(1.0) / (h.gamma0 - Real(1.0));
-  const Real ekin = (Real(0.5) * qg[ID]) * ((qg[IU] * qg[IU]) + (qg[IV] * qg[IV]));
-  const Real etot = (qg[IP] * entho) + ekin;
+  const Real ekin = O::half(qg[ID]) * ((qg[IU] * qg[IU]) + (qg[IV] * qg[IV]));
+  const Real etot = (qg[IP] * h.entho) + ekin;
   flux[IP] = qg[IU] * (etot + qg[IP]);
 }
 
@@ -148,57 +224,59 @@ __device__ __forceinline__ void cmpflx(const Hydro<Real>& h, const Real qg[4], R
 template <typename Real>
 __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real qleft[4],
                                                const Real qright[4], Real flux[4]) {
-  const Real ONE = Real(1.0), ZERO = Real(0.0), H = Real(0.5);
+  using O = Ops<Real>;
+  const Real ONE = Real(1.0), ZERO = Real(0.0);
   const Real tol = Real(1e-6f);
-  const Real rl = rmax(qleft[ID], h.smallr);
+  const Real rl = O::max(qleft[ID], h.smallr);
   const Real ul = qleft[IU];
-  const Real pl = rmax(qleft[IP], rl * h.smallp);
-  const Real rr = rmax(qright[ID], h.smallr);
+  const Real pl = O::max(qleft[IP], rl * h.smallp);
+  const Real rr = O::max(qright[ID], h.smallr);
   const Real ur = qright[IU];
-  const Real pr = rmax(qright[IP], rr * h.smallp);
+  const Real pr = O::max(qright[IP], rr * h.smallp);
   const Real cl = (h.gamma0 * pl) * rl;
   const Real cr = (h.gamma0 * pr) * rr;
-  Real wl = rsqrt_ieee(cl);
-  Real wr = rsqrt_ieee(cr);
-  Real pold = rmax((((wr * pl) + (wl * pr)) + ((wl * wr) * (ul - ur))) / (wl + wr), ZERO);
+  Real wl = O::sqrt(cl);
+  Real wr = O::sqrt(cr);
+  Real pold = O::max(O::div(((wr * pl) + (wl * pr)) + ((wl * wr) * (ul - ur)), wl + wr), ZERO);
   Real conv = ONE;
   int iter = 0;
-  while (iter < h.niter_riemann && conv > tol) {
-    const Real wwl = rsqrt_ieee(cl * (ONE + ((h.gamma6 * (pold - pl)) / pl)));
-    const Real wwr = rsqrt_ieee(cr * (ONE + ((h.gamma6 * (pold - pr)) / pr)));
-    const Real ql = (((Real(2.0) * wwl) * wwl) * wwl) / ((wwl * wwl) + cl);
-    const Real qr = (((Real(2.0) * wwr) * wwr) * wwr) / ((wwr * wwr) + cr);
-    const Real usl = ul - ((pold - pl) / wwl);
-    const Real usr = ur + ((pold - pr) / wwr);
-    const Real delp = rmax(((qr * ql) / (qr + ql)) * (usl - usr), -pold);
+  while (iter < h.niter_riemann && O::gt(conv, tol)) {
+    const Real wwl = O::sqrt(cl * (ONE + O::div(h.gamma6 * (pold - pl), pl)));
+    const Real wwr = O::sqrt(cr * (ONE + O::div(h.gamma6 * (pold - pr), pr)));
+    const Real ql = O::div((O::twice(wwl) * wwl) * wwl, (wwl * wwl) + cl);
+    const Real qr = O::div((O::twice(wwr) * wwr) * wwr, (wwr * wwr) + cr);
+    const Real usl = ul - O::div(pold - pl, wwl);
+    const Real usr = ur + O::div(pold - pr, wwr);
+    const Real delp = O::max(O::div(qr * ql, qr + ql) * (usl - usr), -pold);
     pold = pold + delp;
-    conv = rabs(delp / (pold + h.smallpp));
+    conv = rabs(O::div(delp, pold + h.smallpp));
     iter = iter + 1;
   }
   const Real pstar = pold;
-  wl = rsqrt_ieee(cl * (ONE + ((h.gamma6 * (pstar - pl)) / pl)));
-  wr = rsqrt_ieee(cr * (ONE + ((h.gamma6 * (pstar - pr)) / pr)));
-  const Real ustar = H * ((((ul + ((pl - pstar) / wl)) + ur) - ((pr - pstar) / wr)));
-  const Real sgnm = (ustar >= ZERO) ? ONE : -ONE;
+  wl = O::sqrt(cl * (ONE + O::div(h.gamma6 * (pstar - pl), pl)));
+  wr = O::sqrt(cr * (ONE + O::div(h.gamma6 * (pstar - pr), pr)));
+  const Real ustar = O::half(((ul + O::div(pl - pstar, wl)) + ur) - O::div(pr - pstar, wr));
+  const bool left = O::ge0(ustar);  // sgnm = +1 (else -1)
   Real ro, uo, po, wo;
-  if (sgnm > ZERO) { ro = rl; uo = ul; po = pl; wo = wl; }
-  else             { ro = rr; uo = ur; po = pr; wo = wr; }
-  const Real co = rmax(h.smallc, rsqrt_ieee(rabs((h.gamma0 * po) / ro)));
-  const Real rstar = rmax(ro / (ONE + ((ro * (po - pstar)) / (wo * wo))), h.smallr);
-  const Real cstar = rmax(h.smallc, rsqrt_ieee(rabs((h.gamma0 * pstar) / rstar)));
-  Real spout = co - (sgnm * uo);
-  Real spin = cstar - (sgnm * ustar);
-  const Real ushock = (wo / ro) - (sgnm * uo);
-  if (pstar >= po) { spin = ushock; spout = ushock; }
-  const Real scr = rmax(spout - spin, h.smallc + rabs(spout + spin));
-  const Real frac = H * (ONE + ((spout + spin) / scr));
+  if (left) { ro = rl; uo = ul; po = pl; wo = wl; }
+  else      { ro = rr; uo = ur; po = pr; wo = wr; }
+  const Real co = O::max(h.smallc, O::sqrt(rabs(O::div(h.gamma0 * po, ro))));
+  const Real rstar = O::max(O::div(ro, ONE + O::div(ro * (po - pstar), wo * wo)), h.smallr);
+  const Real cstar = O::max(h.smallc, O::sqrt(rabs(O::div(h.gamma0 * pstar, rstar))));
+  const Real suo = O::neg_if(uo, !left), sust = O::neg_if(ustar, !left);  // sgnm*uo, sgnm*ustar
+  Real spout = co - suo;
+  Real spin = cstar - sust;
+  const Real ushock = O::div(wo, ro) - suo;
+  if (O::ge(pstar, po)) { spin = ushock; spout = ushock; }
+  const Real scr = O::max(spout - spin, h.smallc + rabs(spout + spin));
+  const Real frac = O::half(ONE + O::div(spout + spin, scr));
   Real qg[4];
   qg[ID] = (frac * rstar) + ((ONE - frac) * ro);
   qg[IU] = (frac * ustar) + ((ONE - frac) * uo);
   qg[IP] = (frac * pstar) + ((ONE - frac) * po);
-  if (spout < ZERO) { qg[ID] = ro; qg[IU] = uo; qg[IP] = po; }
-  if (spin > ZERO) { qg[ID] = rstar; qg[IU] = ustar; qg[IP] = pstar; }
-  qg[IV] = (sgnm > ZERO) ? qleft[IV] : qright[IV];
+  if (O::lt0(spout)) { qg[ID] = ro; qg[IU] = uo; qg[IP] = po; }
+  if (O::gt0(spin)) { qg[ID] = rstar; qg[IU] = ustar; qg[IP] = pstar; }
+  qg[IV] = left ? qleft[IV] : qright[IV];
   cmpflx(h, qg, flux);
 }
 
@@ -206,48 +284,50 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
 template <typename Real>
 __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real qleft[4],
                                              const Real qright[4], Real flux[4]) {
-  const Real ONE = Real(1.0), ZERO = Real(0.0), H = Real(0.5);
-  const Real entho = ONE / (h.gamma0 - ONE);
-  const Real rl = rmax(qleft[ID], h.smallr);
-  const Real pl = rmax(qleft[IP], rl * h.smallp);
+  using O = Ops<Real>;
+  const Real rl = O::max(qleft[ID], h.smallr);
+  const Real pl = O::max(qleft[IP], rl * h.smallp);
   const Real ul = qleft[IU];
-  Real ecinl = ((H * rl) * ul) * ul;
-  ecinl = ecinl + (((H * rl) * qleft[IV]) * qleft[IV]);
-  const Real etotl = (pl * entho) + ecinl;
+  const Real hrl = O::half(rl);
+  Real ecinl = (hrl * ul) * ul;
+  ecinl = ecinl + ((hrl * qleft[IV]) * qleft[IV]);
+  const Real etotl = (pl * h.entho) + ecinl;
   const Real ptotl = pl;
-  const Real rr = rmax(qright[ID], h.smallr);
-  const Real pr = rmax(qright[IP], rr * h.smallp);
+  const Real rr = O::max(qright[ID], h.smallr);
+  const Real pr = O::max(qright[IP], rr * h.smallp);
   const Real ur = qright[IU];
-  Real ecinr = ((H * rr) * ur) * ur;
-  ecinr = ecinr + (((H * rr) * qright[IV]) * qright[IV]);
-  const Real etotr = (pr * entho) + ecinr;
+  const Real hrr = O::half(rr);
+  Real ecinr = (hrr * ur) * ur;
+  ecinr = ecinr + ((hrr * qright[IV]) * qright[IV]);
+  const Real etotr = (pr * h.entho) + ecinr;
   const Real ptotr = pr;
-  const Real cfastl = rsqrt_ieee(rmax((h.gamma0 * pl) / rl, h.smallc * h.smallc));
-  const Real cfastr = rsqrt_ieee(rmax((h.gamma0 * pr) / rr, h.smallc * h.smallc));
-  const Real SL = rmin(ul, ur) - rmax(cfastl, cfastr);
-  const Real SR = rmax(ul, ur) + rmax(cfastl, cfastr);
+  const Real cfastl = O::sqrt(O::max(O::div(h.gamma0 * pl, rl), h.smallc2));
+  const Real cfastr = O::sqrt(O::max(O::div(h.gamma0 * pr, rr), h.smallc2));
+  const Real cmax = O::max(cfastl, cfastr);
+  const Real SL = O::min(ul, ur) - cmax;
+  const Real SR = O::max(ul, ur) + cmax;
   const Real rcl = rl * (ul - SL);
   const Real rcr = rr * (SR - ur);
-  const Real ustar = (((rcr * ur) + (rcl * ul)) + (ptotl - ptotr)) / (rcr + rcl);
-  const Real ptotstar = (((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur))) / (rcr + rcl);
+  const Real ustar = O::div(((rcr * ur) + (rcl * ul)) + (ptotl - ptotr), rcr + rcl);
+  const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
   Real ro, uo, ptoto, etoto;
-  if (SL > ZERO) {
+  if (O::gt0(SL)) {
     ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
-  } else if (ustar > ZERO) {
-    ro = (rl * (SL - ul)) / (SL - ustar);
+  } else if (O::gt0(ustar)) {
+    ro = O::div(rl * (SL - ul), SL - ustar);
     uo = ustar; ptoto = ptotstar;
-    etoto = ((((SL - ul) * etotl) - (ptotl * ul)) + (ptotstar * ustar)) / (SL - ustar);
-  } else if (SR > ZERO) {
-    ro = (rr * (SR - ur)) / (SR - ustar);
+    etoto = O::div((((SL - ul) * etotl) - (ptotl * ul)) + (ptotstar * ustar), SL - ustar);
+  } else if (O::gt0(SR)) {
+    ro = O::div(rr * (SR - ur), SR - ustar);
     uo = ustar; ptoto = ptotstar;
-    etoto = ((((SR - ur) * etotr) - (ptotr * ur)) + (ptotstar * ustar)) / (SR - ustar);
+    etoto = O::div((((SR - ur) * etotr) - (ptotr * ur)) + (ptotstar * ustar), SR - ustar);
   } else {
     ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
   }
   flux[ID] = ro * uo;
   flux[IU] = ((ro * uo) * uo) + ptoto;
   flux[IP] = (etoto + ptoto) * uo;
-  flux[IV] = (flux[ID] > ZERO) ? (flux[ID] * qleft[IV]) : (flux[ID] * qright[IV]);
+  flux[IV] = O::gt0(flux[ID]) ? (flux[ID] * qleft[IV]) : (flux[ID] * qright[IV]);
 }
 
 template <typename Real>
