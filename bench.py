@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -54,6 +55,12 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=200)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-nx", type=int, default=512)
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--adjoint-batch-steps", type=int, default=100)
     return ap.parse_args()
 
 
@@ -230,6 +237,98 @@ def run_reference(a, dist):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- batched ensemble
+
+def measure_batched(E, a):
+    """64 seeded problems (sides 128..1024, offsets, states and walls at random)
+    advanced together by one launch per step from a captured graph, against the
+    same problems advanced one after another with the single-run kernel."""
+    from euler2d_cudafortran_gb300.ensemble import diagonal_ensemble
+    ens = diagonal_ensemble(64, 12345)
+    n = a.batched_steps
+    riemann = E.RIEMANN_HLLC if a.riemann == "hllc" else E.RIEMANN_APPROX
+    init = (ens.offset, ens.rho_hi, ens.p_hi, ens.rho_lo, ens.p_lo)
+    with E.Batch(ens.sizes, ens.bcs, gamma0=1.4, cfl=0.8, riemann_solver=riemann, precision=a.precision) as b:
+        b.init_diagonal(*init)
+        t0 = time.perf_counter()
+        b.tune(steps=3)
+        tune_s = time.perf_counter() - t0
+        sched = b.schedule()
+        b.advance(0, n, log=False)  # captures the graph of the timed sequence
+        b.init_diagonal(*init)
+        b.advance(0, n, log=False)
+        batched_ms = b.last_advance_ms()
+        health = [b.health(k) for k in range(b.nprob)]
+    plain_ms = 0.0
+    for k, (nx, ny) in enumerate(ens.sizes):
+        bc = ens.bcs[k]
+        p = E.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=riemann, precision=a.precision,
+                          boundary_type_xmin=bc[0], boundary_type_xmax=bc[1], boundary_type_ymin=bc[2],
+                          boundary_type_ymax=bc[3])
+        with E.HydroRun(p) as run:
+            run.init_diagonal(*(x[k] for x in init))
+            run.advance(0, n, log=False)
+            plain_ms += run.last_advance_ms()
+    cells = ens.cells
+    return {"workload": f"64 problems, sides uniform in {{128..1024 step 64}} (total {cells} cells), "
+                        f"seed 12345, {n} steps per graph", "steps": n,
+            "mcells_per_s": round(cells * n / (batched_ms * 1e-3) / 1e6, 2),
+            "plain_problem_by_problem_mcells_per_s": round(cells * n / (plain_ms * 1e-3) / 1e6, 2),
+            "speedup_vs_problem_by_problem": round(plain_ms / batched_ms, 3),
+            "batched_ms": round(batched_ms, 3), "plain_ms": round(plain_ms, 3),
+            "schedule": sched, "autotune_s": round(tune_s, 2), "health_flags_nonzero": int(sum(1 for h in health if h))}
+
+
+# ---------------------------------------------------------------- adjoints
+
+def measure_adjoint(E, a):
+    """dJ/d(initial density) of J = sum rho^2 w (Gaussian of width 0.1 at
+    (0.6, 0.6)) on the diagonal-interface problem, FP64 HLLC: the gradient
+    (forward with sqrt(N) checkpoints, recomputation and reverse sweep, one
+    captured graph) against the forward run alone."""
+    n, ns = a.adjoint_nx, a.adjoint_steps
+    p = E.make_params(nx=n, ny=n, gamma0=1.4, cfl=0.8, riemann_solver=E.RIEMANN_HLLC)
+    with E.Adjoint(p) as A:
+        A.gradient(ns, dt_mode=1)  # captures the graph
+        grads = []
+        for _ in range(3):
+            A.gradient(ns, dt_mode=1)
+            grads.append(A.last_ms()[1])
+        fwd = []
+        for _ in range(3):
+            A.objective(ns)
+            fwd.append(A.last_ms()[0])
+    g, f = min(grads), min(fwd)
+    return {"workload": f"{n}x{n} FP64 HLLC, {ns} steps, dt through the running CFL maximum, "
+                        f"checkpoints every {math.ceil(math.sqrt(ns))} steps",
+            "gradient_ms": round(g, 3), "forward_ms": round(f, 3), "adjoint_over_forward": round(g / f, 3),
+            "forward_mcells_per_s": round(n * n * ns / (f * 1e-3) / 1e6, 2)}
+
+
+def measure_adjoint_batch(E, a):
+    """32 seeded problems (sides 256..1024, states and walls as the ensemble
+    workload), FP64 HLLC, per-problem gradients from one forward/backward
+    graph; the forward-only graph of the same batch beside it."""
+    from euler2d_cudafortran_gb300.ensemble import diagonal_ensemble
+    ens = diagonal_ensemble(32, 2024, sides=tuple(range(256, 1025, 64)))
+    ns = a.adjoint_batch_steps
+    init = (ens.offset, ens.rho_hi, ens.p_hi, ens.rho_lo, ens.p_lo)
+    with E.AdjointBatch(ens.sizes, ens.bcs, gamma0=1.4, cfl=0.8) as B:
+        B.init_diagonal(*init)
+        B.gradient(ns, dt_mode=1)  # captures the graph
+        B.gradient(ns, dt_mode=1)
+        g = B.last_ms()[1]
+        B.objective(ns)
+        B.objective(ns)
+        f = B.last_ms()[0]
+    cells = ens.cells
+    return {"workload": f"32 problems, sides uniform in {{256..1024 step 64}} (total {cells} cells), seed 2024, "
+                        f"{ns} steps, dt through the running CFL maximum",
+            "gradient_ms": round(g, 3), "forward_ms": round(f, 3), "adjoint_over_forward": round(g / f, 3),
+            "gradients_per_s": round(32 / (g * 1e-3), 3),
+            "forward_mcells_per_s": round(cells * ns / (f * 1e-3) / 1e6, 2)}
+
+
 # ---------------------------------------------------------------- our arm
 
 def run_ours(a, dist):
@@ -344,6 +443,14 @@ def run_ours(a, dist):
             variants.append({"nx": nx, "precision": "FP64" if prec == 8 else "FP32", "implementationVersion": ver,
                              "steps": ns, "mcells_per_s": round(nx * nx * ns / (vms * 1e-3) / 1e6, 2)})
 
+    batched = None
+    if dist.rank == 0 and not a.no_batched:
+        batched = measure_batched(E, a)
+    adjoint = adjoint_batch = None
+    if dist.rank == 0 and not a.no_adjoint:
+        adjoint = measure_adjoint(E, a)
+        adjoint_batch = measure_adjoint_batch(E, a)
+
     if dist.rank == 0:
         isz = a.nx + 4
         line = {
@@ -370,6 +477,9 @@ def run_ours(a, dist):
             "gpu_launches": a.steps + 1 if a.version == 0 else 4 * a.steps,
             "health_flags": health,
             "variants": variants,
+            "batched": batched,
+            "adjoint": adjoint,
+            "adjoint_batched": adjoint_batch,
         }
         print(json.dumps(line), flush=True)
 

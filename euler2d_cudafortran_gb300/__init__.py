@@ -49,6 +49,14 @@ EXPORTED_SYMBOLS = [
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
     "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
     "e2d_godunov_unsplit_noalloc", "e2d_selftest_arith",
+    "e2d_batch_create", "e2d_batch_destroy", "e2d_batch_init_diagonal", "e2d_batch_upload_state",
+    "e2d_batch_download_state", "e2d_batch_advance", "e2d_batch_last_advance_ms", "e2d_batch_set_schedule",
+    "e2d_batch_get_schedule", "e2d_batch_tune", "e2d_batch_get_health",
+    "e2d_adjoint_create", "e2d_adjoint_destroy", "e2d_adjoint_objective", "e2d_adjoint_gradient",
+    "e2d_adjoint_last_ms",
+    "e2d_adjoint_batch_create", "e2d_adjoint_batch_destroy", "e2d_adjoint_batch_init_diagonal",
+    "e2d_adjoint_batch_upload_state", "e2d_adjoint_batch_objective", "e2d_adjoint_batch_gradient",
+    "e2d_adjoint_batch_last_ms",
 ]
 
 
@@ -112,6 +120,32 @@ def load_library(path: str = LIB_PATH):
                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double)],
     }
+    dp = ctypes.POINTER(ctypes.c_double)
+    sig.update({
+        "e2d_batch_create": [ctypes.POINTER(Params), i, ip, ip, ip, ctypes.POINTER(vp)],
+        "e2d_batch_destroy": [vp],
+        "e2d_batch_init_diagonal": [vp, dp, dp, dp, dp, dp],
+        "e2d_batch_upload_state": [vp, i, i, vp],
+        "e2d_batch_download_state": [vp, i, i, vp],
+        "e2d_batch_advance": [vp, i, i, vp],
+        "e2d_batch_last_advance_ms": [vp, ctypes.POINTER(ctypes.c_float)],
+        "e2d_batch_set_schedule": [vp, i, i, i],
+        "e2d_batch_get_schedule": [vp, ip, ip, ip, ip],
+        "e2d_batch_tune": [vp, i, ctypes.c_char_p, ctypes.POINTER(ctypes.c_float)],
+        "e2d_batch_get_health": [vp, i, ctypes.POINTER(ctypes.c_uint)],
+        "e2d_adjoint_create": [ctypes.POINTER(Params), ctypes.POINTER(vp)],
+        "e2d_adjoint_destroy": [vp],
+        "e2d_adjoint_objective": [vp, vp, i, d, d, d, dp, dp],
+        "e2d_adjoint_gradient": [vp, vp, i, i, d, d, d, dp, dp, dp],
+        "e2d_adjoint_last_ms": [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+        "e2d_adjoint_batch_create": [ctypes.POINTER(Params), i, ip, ip, ip, ctypes.POINTER(vp)],
+        "e2d_adjoint_batch_destroy": [vp],
+        "e2d_adjoint_batch_init_diagonal": [vp, dp, dp, dp, dp, dp],
+        "e2d_adjoint_batch_upload_state": [vp, i, vp],
+        "e2d_adjoint_batch_objective": [vp, i, d, d, d, dp],
+        "e2d_adjoint_batch_gradient": [vp, i, i, d, d, d, dp, dp, dp],
+        "e2d_adjoint_batch_last_ms": [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+    })
     for name, args in sig.items():
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -254,6 +288,237 @@ class HydroRun:
     def final_state(self, nsteps: int) -> np.ndarray:
         """The state after nsteps steps from u: u if nsteps is even, else u2."""
         return self.get_state(nsteps % 2)
+
+
+class Batch:
+    """An ensemble of independent runs advanced together (e2d_batch_*)."""
+
+    def __init__(self, sizes, bcs=None, params: Params | None = None, **kw):
+        self._lib = load_library()
+        self.params = params if params is not None else make_params(**kw)
+        self.sizes = [(int(a), int(b)) for a, b in sizes]
+        n = len(self.sizes)
+        nx = (ctypes.c_int * n)(*[a for a, _ in self.sizes])
+        ny = (ctypes.c_int * n)(*[b for _, b in self.sizes])
+        bc = None
+        if bcs is not None:
+            flat = [int(x) for row in bcs for x in (row if hasattr(row, "__len__") else (row,) * 4)]
+            bc = (ctypes.c_int * len(flat))(*flat)
+        h = ctypes.c_void_p()
+        _check(self._lib.e2d_batch_create(ctypes.byref(self.params), n, nx, ny, bc, ctypes.byref(h)))
+        self._h = h
+        self.nprob = n
+        self.dtype = np.float64 if self.params.precision == 8 else np.float32
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.e2d_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_diagonal(self, offset, rho_hi, p_hi, rho_lo, p_lo):
+        arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (self.nprob,)))
+                for x in (offset, rho_hi, p_hi, rho_lo, p_lo)]
+        ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrs]
+        _check(self._lib.e2d_batch_init_diagonal(self._h, *ptrs))
+
+    def get_state(self, prob: int, which: int) -> np.ndarray:
+        nx, ny = self.sizes[prob]
+        a = np.zeros((4, ny + 4, nx + 4), dtype=self.dtype)
+        _check(self._lib.e2d_batch_download_state(self._h, prob, which, a.ctypes.data_as(ctypes.c_void_p)))
+        return a
+
+    def set_state(self, prob: int, which: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        _check(self._lib.e2d_batch_upload_state(self._h, prob, which, a.ctypes.data_as(ctypes.c_void_p)))
+
+    def advance(self, nStep0: int, nsteps: int, log: bool = True):
+        buf = np.zeros((max(nsteps, 1), self.nprob), dtype=self.dtype) if log else None
+        _check(self._lib.e2d_batch_advance(self._h, nStep0, nsteps,
+                                           buf.ctypes.data_as(ctypes.c_void_p) if log else None))
+        return buf[:nsteps] if log else None
+
+    def last_advance_ms(self) -> float:
+        ms = ctypes.c_float()
+        _check(self._lib.e2d_batch_last_advance_ms(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def set_schedule(self, variant: int, grid_mult: int, order: int):
+        _check(self._lib.e2d_batch_set_schedule(self._h, variant, grid_mult, order))
+
+    def schedule(self):
+        v, m, o, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.e2d_batch_get_schedule(self._h, ctypes.byref(v), ctypes.byref(m), ctypes.byref(o),
+                                                ctypes.byref(g)))
+        return {"tile": ["32x15", "32x7"][v.value], "variant": v.value, "grid_mult": m.value,
+                "order": ["problem", "largest-first"][o.value], "grid": g.value}
+
+    def tune(self, steps: int = 3, cache_path: str | None = None) -> float:
+        ms = ctypes.c_float()
+        _check(self._lib.e2d_batch_tune(self._h, steps, cache_path.encode() if cache_path else None,
+                                        ctypes.byref(ms)))
+        return ms.value
+
+    def health(self, prob: int) -> int:
+        x = ctypes.c_uint()
+        _check(self._lib.e2d_batch_get_health(self._h, prob, ctypes.byref(x)))
+        return x.value
+
+    def final_state(self, prob: int, nsteps: int) -> np.ndarray:
+        return self.get_state(prob, nsteps % 2)
+
+
+class Adjoint:
+    """Discrete adjoint of the FP64 HLLC step: J = sum rho^2 w(x, y) after
+    nsteps steps and dJ/d(initial interior density) (e2d_adjoint_*)."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self._lib = load_library()
+        kw.setdefault("riemann_solver", RIEMANN_HLLC)
+        self.params = params if params is not None else make_params(**kw)
+        h = ctypes.c_void_p()
+        _check(self._lib.e2d_adjoint_create(ctypes.byref(self.params), ctypes.byref(h)))
+        self._h = h
+        self.nx, self.ny = self.params.nx, self.params.ny
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.e2d_adjoint_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _u0(u0):
+        if u0 is None:
+            return None, None
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        return a, a.ctypes.data_as(ctypes.c_void_p)
+
+    def objective(self, nsteps, u0=None, xc=0.6, yc=0.6, sigma=0.1, dt_fixed=None) -> float:
+        keep, ptr = self._u0(u0)
+        J = ctypes.c_double()
+        dtp = None
+        if dt_fixed is not None:
+            dtf = np.ascontiguousarray(dt_fixed, dtype=np.float64)
+            dtp = dtf.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        _check(self._lib.e2d_adjoint_objective(self._h, ptr, nsteps, xc, yc, sigma, dtp, ctypes.byref(J)))
+        return J.value
+
+    def gradient(self, nsteps, u0=None, dt_mode=1, xc=0.6, yc=0.6, sigma=0.1):
+        """Returns (J, dJ/drho0 as (ny, nx), dt of every step)."""
+        keep, ptr = self._u0(u0)
+        J = ctypes.c_double()
+        g = np.zeros((self.ny, self.nx), dtype=np.float64)
+        dts = np.zeros(nsteps, dtype=np.float64)
+        _check(self._lib.e2d_adjoint_gradient(self._h, ptr, nsteps, dt_mode, xc, yc, sigma, ctypes.byref(J),
+                                              g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                              dts.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return J.value, g, dts
+
+    def last_ms(self):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(self._lib.e2d_adjoint_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+
+class AdjointBatch:
+    """The discrete adjoint of an ensemble of FP64 HLLC problems of uneven
+    sizes, all stages batched, one captured graph per call
+    (e2d_adjoint_batch_*)."""
+
+    def __init__(self, sizes, bcs=None, params: Params | None = None, **kw):
+        self._lib = load_library()
+        kw.setdefault("riemann_solver", RIEMANN_HLLC)
+        self.params = params if params is not None else make_params(**kw)
+        self.sizes = [(int(a), int(b)) for a, b in sizes]
+        n = len(self.sizes)
+        nx = (ctypes.c_int * n)(*[a for a, _ in self.sizes])
+        ny = (ctypes.c_int * n)(*[b for _, b in self.sizes])
+        bc = None
+        if bcs is not None:
+            flat = [int(x) for row in bcs for x in (row if hasattr(row, "__len__") else (row,) * 4)]
+            bc = (ctypes.c_int * len(flat))(*flat)
+        h = ctypes.c_void_p()
+        _check(self._lib.e2d_adjoint_batch_create(ctypes.byref(self.params), n, nx, ny, bc, ctypes.byref(h)))
+        self._h = h
+        self.nprob = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.e2d_adjoint_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_diagonal(self, offset, rho_hi, p_hi, rho_lo, p_lo):
+        arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (self.nprob,)))
+                for x in (offset, rho_hi, p_hi, rho_lo, p_lo)]
+        ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrs]
+        _check(self._lib.e2d_adjoint_batch_init_diagonal(self._h, *ptrs))
+
+    def set_state(self, prob, u0):
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        nx, ny = self.sizes[prob]
+        if a.shape != (4, ny + 4, nx + 4):
+            raise ValueError(f"state of problem {prob} must have shape {(4, ny + 4, nx + 4)}")
+        _check(self._lib.e2d_adjoint_batch_upload_state(self._h, prob, a.ctypes.data_as(ctypes.c_void_p)))
+
+    def objective(self, nsteps, xc=0.6, yc=0.6, sigma=0.1):
+        J = np.zeros(self.nprob)
+        _check(self._lib.e2d_adjoint_batch_objective(self._h, nsteps, xc, yc, sigma,
+                                                     J.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return J
+
+    def gradient(self, nsteps, dt_mode=1, xc=0.6, yc=0.6, sigma=0.1):
+        """Returns (J[nprob], [dJ_p/drho0_p as (ny_p, nx_p)], dt log (nsteps, nprob))."""
+        J = np.zeros(self.nprob)
+        g = np.zeros(sum(a * b for a, b in self.sizes))
+        dts = np.zeros((nsteps, self.nprob))
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(self._lib.e2d_adjoint_batch_gradient(self._h, nsteps, dt_mode, xc, yc, sigma, J.ctypes.data_as(dp),
+                                                    g.ctypes.data_as(dp), dts.ctypes.data_as(dp)))
+        grads, o = [], 0
+        for nx, ny in self.sizes:
+            grads.append(g[o:o + nx * ny].reshape(ny, nx))
+            o += nx * ny
+        return J, grads, dts
+
+    def last_ms(self):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(self._lib.e2d_adjoint_batch_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
 
 def measure_fp64_peak():

@@ -26,7 +26,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libeuler2d_gb300.so")
 EXE = os.path.join(OUT, "euler2d_gb300")
 
-CUDA_SOURCES = ["abi.cu", "k_sweeps.cu", "k_fused.cu", "k_probe.cu", "noalloc.cu", "k_selftest.cu"]
+CUDA_SOURCES = ["abi.cu", "k_sweeps.cu", "k_fused.cu", "k_probe.cu", "noalloc.cu", "k_selftest.cu", "k_batch.cu", "abi_batch.cu", "k_adjoint.cu", "abi_adjoint.cu", "abi_adjoint_batch.cu"]
 DRIVER_SOURCES = ["main.cpp", "namelist.cpp", "vtk.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",

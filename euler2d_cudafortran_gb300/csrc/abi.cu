@@ -101,6 +101,7 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
   Field<Real> out = field<Real>(r, even ? r->u2 : r->u);
   StepDt<Real> sd;
   sd.dt_value = dt_value;
+  sd.dt_ptr = nullptr;
   sd.from_slot = from_slot ? 1 : 0;
   sd.rd_slot = rd;
   sd.wr_slot = wr;

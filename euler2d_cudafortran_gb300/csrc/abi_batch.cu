@@ -1,0 +1,455 @@
+// abi_batch.cu -- C ABI of the batched ensemble (e2d_batch_*): many
+// independent runs of uneven sizes advanced together, each with its own dt,
+// by one kernel launch per step, steps replayed from captured CUDA graphs,
+// with a schedule (tile shape, grid size, tile order) chosen by an autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/euler2d_gb300.h"
+#include "batch.h"
+#include "hydro_params.h"
+
+using namespace e2d;
+
+struct e2d_batch {
+  int nprob = 0, es = 8, device = 0;
+  std::vector<e2d_params> params;
+  std::vector<Hydro<double>> hd;
+  std::vector<Hydro<float>> hf;
+  std::vector<size_t> pitch, plane, off;  // elements
+  size_t pool_elems = 0;
+  void* pool_u = nullptr;
+  void* pool_u2 = nullptr;
+  Ctl* ctls = nullptr;
+  void* d_probs = nullptr;  // BatchProb<Real>[nprob], work-list order
+  void* d_dtlog = nullptr;
+  int dtlog_cap = 0;
+  int variant = 0, mult = 1, order = 1;  // schedule
+  int total_tiles = 0, grid = 0;
+  int cur_slot = 0;
+  bool folded = false;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timed = false;
+  std::map<std::tuple<int, int, int, int, int, int, int>, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+int bfail(int code, const std::string& msg) { return set_error(code, msg); }
+
+#define B_CK(call)                                                                         \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return bfail(E2D_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename Real> const Hydro<Real>& bh(const e2d_batch* b, int p);
+template <> const Hydro<double>& bh<double>(const e2d_batch* b, int p) { return b->hd[p]; }
+template <> const Hydro<float>& bh<float>(const e2d_batch* b, int p) { return b->hf[p]; }
+
+template <typename Real>
+Field<Real> bfield(const e2d_batch* b, int p, int which) {
+  Real* base = static_cast<Real*>(which ? b->pool_u2 : b->pool_u);
+  return Field<Real>{base + b->off[p], (int)b->pitch[p], (long long)b->plane[p]};
+}
+
+void clear_graphs(e2d_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+// Lay out the flattened tile list for the current schedule and upload it.
+template <typename Real>
+int build_worklist(e2d_batch* b) {
+  int tx, ty, nt;
+  batch_tile_shape<Real>(b->variant, &tx, &ty, &nt);
+  std::vector<int> order(b->nprob);
+  std::iota(order.begin(), order.end(), 0);
+  if (b->order == 1)  // largest problems first
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+      return (long long)b->params[a].nx * b->params[a].ny > (long long)b->params[c].nx * b->params[c].ny;
+    });
+  std::vector<BatchProb<Real>> probs(b->nprob);
+  int t = 0;
+  for (int k = 0; k < b->nprob; ++k) {
+    const int p = order[k];
+    BatchProb<Real>& P = probs[k];
+    P.h = bh<Real>(b, p);
+    P.u = bfield<Real>(b, p, 0).p;
+    P.u2 = bfield<Real>(b, p, 1).p;
+    P.pitch = (int)b->pitch[p];
+    P.plane = (long long)b->plane[p];
+    P.ntx = (b->params[p].nx + tx - 1) / tx;
+    P.nty = (b->params[p].ny + ty - 1) / ty;
+    P.tile_begin = t;
+    P.id = p;
+    t += P.ntx * P.nty;
+  }
+  b->total_tiles = t;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int res = std::max(1, batch_resident_per_sm<Real>(b->variant));
+  b->grid = std::max(1, std::min(t, sms * res * b->mult));
+  if (!b->d_probs) B_CK(cudaMalloc(&b->d_probs, sizeof(BatchProb<double>) * (size_t)b->nprob));
+  B_CK(cudaMemcpyAsync(b->d_probs, probs.data(), sizeof(BatchProb<Real>) * (size_t)b->nprob,
+                       cudaMemcpyHostToDevice, b->stream));
+  B_CK(cudaStreamSynchronize(b->stream));
+  clear_graphs(b);
+  return E2D_OK;
+}
+
+int build(e2d_batch* b) { return b->es == 8 ? build_worklist<double>(b) : build_worklist<float>(b); }
+
+template <typename Real>
+void enqueue(e2d_batch* b, int nStep0, int nsteps, int slot0, bool seed) {
+  for (int p = 0; p < b->nprob; ++p) {
+    Field<Real> cur = bfield<Real>(b, p, nStep0 % 2);
+    if (seed) launch_dt_reduce<Real>(bh<Real>(b, p), cur, &b->ctls[p], slot0, b->stream);
+    launch_boundaries<Real>(bh<Real>(b, p), cur, b->stream);
+  }
+  for (int k = 0; k < nsteps; ++k) {
+    BatchLaunch<Real> L;
+    L.probs = static_cast<const BatchProb<Real>*>(b->d_probs);
+    L.nprob = b->nprob;
+    L.total_tiles = b->total_tiles;
+    L.parity = (nStep0 + k) % 2;
+    L.rd = slot0 ^ (k & 1);
+    L.wr = L.rd ^ 1;
+    L.grid = b->grid;
+    L.ctls = b->ctls;
+    L.dt_log = static_cast<Real*>(b->d_dtlog) + (size_t)k * b->nprob;
+    launch_batch_step<Real>(b->variant, L, b->stream);
+  }
+}
+
+int check(const e2d_batch* b) { return b ? E2D_OK : bfail(E2D_ERR_INVALID_ARG, "null batch handle"); }
+
+int advance_impl(e2d_batch* b, int nStep0, int nsteps, void* dt_log_host) {
+  if (nsteps <= 0) return E2D_OK;
+  if (nsteps > b->dtlog_cap) {
+    B_CK(cudaStreamSynchronize(b->stream));
+    clear_graphs(b);
+    cudaFree(b->d_dtlog);
+    b->d_dtlog = nullptr;
+    b->dtlog_cap = 0;
+    if (cudaMalloc(&b->d_dtlog, (size_t)nsteps * b->nprob * b->es) != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(E2D_ERR_OOM, "cudaMalloc of the batch dt log failed");
+    }
+    b->dtlog_cap = nsteps;
+  }
+  const int slot0 = b->cur_slot;
+  const bool seed = !b->folded;
+  auto key = std::make_tuple(nStep0 % 2, slot0, nsteps, seed ? 1 : 0, b->variant, b->mult, b->order);
+  cudaGraphExec_t exec = nullptr;
+  auto it = b->graphs.find(key);
+  if (it != b->graphs.end()) {
+    exec = it->second;
+  } else {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      if (b->es == 8) enqueue<double>(b, nStep0, nsteps, slot0, seed);
+      else enqueue<float>(b, nStep0, nsteps, slot0, seed);
+      if (cudaStreamEndCapture(b->stream, &graph) == cudaSuccess && graph) {
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+        cudaGraphDestroy(graph);
+      }
+    }
+    cudaGetLastError();
+    if (exec) {
+      cudaGraphUpload(exec, b->stream);
+      b->graphs[key] = exec;
+    }
+  }
+  B_CK(cudaEventRecord(b->ev0, b->stream));
+  if (exec) {
+    B_CK(cudaGraphLaunch(exec, b->stream));
+  } else {
+    if (b->es == 8) enqueue<double>(b, nStep0, nsteps, slot0, seed);
+    else enqueue<float>(b, nStep0, nsteps, slot0, seed);
+    B_CK(cudaGetLastError());
+  }
+  B_CK(cudaEventRecord(b->ev1, b->stream));
+  b->timed = true;
+  b->cur_slot = slot0 ^ (nsteps & 1);
+  b->folded = true;
+  if (dt_log_host) {
+    B_CK(cudaMemcpyAsync(dt_log_host, b->d_dtlog, (size_t)nsteps * b->nprob * b->es, cudaMemcpyDeviceToHost,
+                         b->stream));
+    B_CK(cudaStreamSynchronize(b->stream));
+  }
+  return E2D_OK;
+}
+
+std::string signature(const e2d_batch* b) {
+  std::ostringstream os;
+  unsigned long long h = 1469598103934665603ull;
+  for (const auto& p : b->params) {
+    h = (h ^ (unsigned long long)p.nx) * 1099511628211ull;
+    h = (h ^ (unsigned long long)p.ny) * 1099511628211ull;
+  }
+  os << "prec" << b->es << "-n" << b->nprob << "-riemann" << b->params[0].riemann_solver << "-" << std::hex << h;
+  return os.str();
+}
+
+}  // namespace
+
+extern "C" {
+
+int e2d_batch_create(const e2d_params* base, int nprob, const int* nx, const int* ny, const int* bc,
+                     e2d_batch** out) {
+  if (!base || !nx || !ny || !out || nprob < 1) return bfail(E2D_ERR_INVALID_ARG, "bad batch arguments");
+  *out = nullptr;
+  if (base->precision != 4 && base->precision != 8) return bfail(E2D_ERR_INVALID_ARG, "precision must be 4 or 8");
+  if (base->riemann_solver != E2D_RIEMANN_APPROX && base->riemann_solver != E2D_RIEMANN_HLLC)
+    return bfail(E2D_ERR_INVALID_ARG, "riemann_solver must be 0 (approx) or 2 (hllc)");
+  if (!(base->gamma0 > 1.0) || !(base->cfl > 0.0) || !(base->smallr > 0.0) || !(base->smallc > 0.0) ||
+      base->niter_riemann < 0)
+    return bfail(E2D_ERR_INVALID_ARG, "gamma0 > 1, cfl > 0, smallr > 0, smallc > 0, niter_riemann >= 0");
+  for (int p = 0; p < nprob; ++p)
+    if (nx[p] < 2 || ny[p] < 2 || nx[p] > (1 << 20) || ny[p] > (1 << 20))
+      return bfail(E2D_ERR_INVALID_ARG, "every nx, ny must be in [2, 2^20]");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return bfail(E2D_ERR_NO_DEVICE, "no CUDA device");
+  }
+  e2d_batch* b = new e2d_batch;
+  b->nprob = nprob;
+  b->es = base->precision;
+  cudaGetDevice(&b->device);
+  size_t total = 0;
+  for (int p = 0; p < nprob; ++p) {
+    e2d_params q = *base;
+    q.nx = nx[p];
+    q.ny = ny[p];
+    if (bc) {
+      q.boundary_type_xmin = bc[4 * p + 0];
+      q.boundary_type_xmax = bc[4 * p + 1];
+      q.boundary_type_ymin = bc[4 * p + 2];
+      q.boundary_type_ymax = bc[4 * p + 3];
+    }
+    b->params.push_back(q);
+    b->hd.push_back(make_hydro<double>(q));
+    b->hf.push_back(make_hydro<float>(q));
+    const size_t pitch = ((size_t)q.nx + 4 + 31) / 32 * 32;
+    const size_t plane = pitch * (size_t)(q.ny + 4);
+    b->pitch.push_back(pitch);
+    b->plane.push_back(plane);
+    b->off.push_back(total);
+    total += 4 * plane;
+  }
+  b->pool_elems = total;
+  auto cleanup = [&](int code, const std::string& m) {
+    e2d_batch_destroy(b);
+    return bfail(code, m);
+  };
+  if (cudaMalloc(&b->pool_u, total * b->es) != cudaSuccess || cudaMalloc(&b->pool_u2, total * b->es) != cudaSuccess ||
+      cudaMalloc(&b->ctls, sizeof(Ctl) * (size_t)nprob) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(E2D_ERR_OOM, "cudaMalloc of the batch states failed");
+  }
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+    return cleanup(E2D_ERR_CUDA, "stream/event creation failed");
+  cudaMemsetAsync(b->pool_u, 0, total * b->es, b->stream);
+  cudaMemsetAsync(b->pool_u2, 0, total * b->es, b->stream);
+  cudaMemsetAsync(b->ctls, 0, sizeof(Ctl) * (size_t)nprob, b->stream);
+  if (int rc = build(b)) return cleanup(rc, "work list setup failed");
+  *out = b;
+  return E2D_OK;
+}
+
+int e2d_batch_destroy(e2d_batch* b) {
+  if (!b) return E2D_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  clear_graphs(b);
+  cudaFree(b->pool_u);
+  cudaFree(b->pool_u2);
+  cudaFree(b->ctls);
+  cudaFree(b->d_probs);
+  cudaFree(b->d_dtlog);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return E2D_OK;
+}
+
+int e2d_batch_init_diagonal(e2d_batch* b, const double* offset, const double* rho_hi, const double* p_hi,
+                            const double* rho_lo, const double* p_lo) {
+  if (int rc = check(b)) return rc;
+  if (!offset || !rho_hi || !p_hi || !rho_lo || !p_lo) return bfail(E2D_ERR_INVALID_ARG, "null initial data");
+  cudaSetDevice(b->device);
+  for (int p = 0; p < b->nprob; ++p) {
+    if (b->es == 8)
+      launch_init_diagonal<double>(b->hd[p], bfield<double>(b, p, 0), offset[p], rho_hi[p], p_hi[p], rho_lo[p],
+                                   p_lo[p], b->stream);
+    else
+      launch_init_diagonal<float>(b->hf[p], bfield<float>(b, p, 0), offset[p], rho_hi[p], p_hi[p], rho_lo[p],
+                                  p_lo[p], b->stream);
+  }
+  B_CK(cudaGetLastError());
+  B_CK(cudaStreamSynchronize(b->stream));
+  b->folded = false;
+  return E2D_OK;
+}
+
+int e2d_batch_upload_state(e2d_batch* b, int prob, int which, const void* host) {
+  if (int rc = check(b)) return rc;
+  if (prob < 0 || prob >= b->nprob || (which != 0 && which != 1) || !host)
+    return bfail(E2D_ERR_INVALID_ARG, "bad upload arguments");
+  cudaSetDevice(b->device);
+  const size_t w = (size_t)(b->params[prob].nx + 4) * b->es;
+  char* dst = static_cast<char*>(which ? b->pool_u2 : b->pool_u) + b->off[prob] * b->es;
+  B_CK(cudaMemcpy2DAsync(dst, b->pitch[prob] * b->es, host, w, w, (size_t)4 * (b->params[prob].ny + 4),
+                         cudaMemcpyHostToDevice, b->stream));
+  B_CK(cudaStreamSynchronize(b->stream));
+  b->folded = false;
+  return E2D_OK;
+}
+
+int e2d_batch_download_state(e2d_batch* b, int prob, int which, void* host) {
+  if (int rc = check(b)) return rc;
+  if (prob < 0 || prob >= b->nprob || (which != 0 && which != 1) || !host)
+    return bfail(E2D_ERR_INVALID_ARG, "bad download arguments");
+  cudaSetDevice(b->device);
+  const size_t w = (size_t)(b->params[prob].nx + 4) * b->es;
+  const char* src = static_cast<const char*>(which ? b->pool_u2 : b->pool_u) + b->off[prob] * b->es;
+  B_CK(cudaMemcpy2DAsync(host, w, src, b->pitch[prob] * b->es, w, (size_t)4 * (b->params[prob].ny + 4),
+                         cudaMemcpyDeviceToHost, b->stream));
+  B_CK(cudaStreamSynchronize(b->stream));
+  return E2D_OK;
+}
+
+int e2d_batch_advance(e2d_batch* b, int nStep0, int nsteps, void* dt_log) {
+  if (int rc = check(b)) return rc;
+  if (nStep0 < 0 || nsteps < 0) return bfail(E2D_ERR_INVALID_ARG, "nStep0 and nsteps must be >= 0");
+  cudaSetDevice(b->device);
+  return advance_impl(b, nStep0, nsteps, dt_log);
+}
+
+int e2d_batch_last_advance_ms(e2d_batch* b, float* ms) {
+  if (int rc = check(b)) return rc;
+  if (!ms || !b->timed) return bfail(E2D_ERR_INVALID_ARG, "no advance has been timed");
+  B_CK(cudaEventSynchronize(b->ev1));
+  B_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+  return E2D_OK;
+}
+
+int e2d_batch_set_schedule(e2d_batch* b, int variant, int grid_mult, int order) {
+  if (int rc = check(b)) return rc;
+  if (variant < 0 || variant > 1 || grid_mult < 1 || grid_mult > 64 || order < 0 || order > 1)
+    return bfail(E2D_ERR_INVALID_ARG, "variant 0|1, grid_mult 1..64, order 0|1");
+  cudaSetDevice(b->device);
+  B_CK(cudaStreamSynchronize(b->stream));
+  b->variant = variant;
+  b->mult = grid_mult;
+  b->order = order;
+  return build(b);
+}
+
+int e2d_batch_get_schedule(e2d_batch* b, int* variant, int* grid_mult, int* order, int* grid) {
+  if (int rc = check(b)) return rc;
+  if (variant) *variant = b->variant;
+  if (grid_mult) *grid_mult = b->mult;
+  if (order) *order = b->order;
+  if (grid) *grid = b->grid;
+  return E2D_OK;
+}
+
+int e2d_batch_tune(e2d_batch* b, int steps, const char* cache_path, float* best_ms) {
+  if (int rc = check(b)) return rc;
+  if (steps < 1) return bfail(E2D_ERR_INVALID_ARG, "steps must be >= 1");
+  cudaSetDevice(b->device);
+  const std::string sig = signature(b);
+  if (cache_path) {  // reuse a previous choice for the same ensemble shape
+    std::ifstream in(cache_path);
+    std::string s;
+    int v, m, o;
+    float t;
+    while (in >> s >> v >> m >> o >> t) {
+      if (s == sig) {
+        if (best_ms) *best_ms = t;
+        return e2d_batch_set_schedule(b, v, m, o);
+      }
+    }
+  }
+  // Save the states and control blocks: tuning advances the problems.
+  const size_t bytes = b->pool_elems * b->es;
+  void *su = nullptr, *su2 = nullptr, *sctl = nullptr;
+  if (cudaMalloc(&su, bytes) != cudaSuccess || cudaMalloc(&su2, bytes) != cudaSuccess ||
+      cudaMalloc(&sctl, sizeof(Ctl) * (size_t)b->nprob) != cudaSuccess) {
+    cudaFree(su);
+    cudaFree(su2);
+    cudaGetLastError();
+    return bfail(E2D_ERR_OOM, "tuning needs a copy of the states");
+  }
+  cudaMemcpyAsync(su, b->pool_u, bytes, cudaMemcpyDeviceToDevice, b->stream);
+  cudaMemcpyAsync(su2, b->pool_u2, bytes, cudaMemcpyDeviceToDevice, b->stream);
+  cudaMemcpyAsync(sctl, b->ctls, sizeof(Ctl) * (size_t)b->nprob, cudaMemcpyDeviceToDevice, b->stream);
+  const int slot_saved = b->cur_slot;
+  const bool folded_saved = b->folded;
+  auto restore = [&]() {
+    cudaMemcpyAsync(b->pool_u, su, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    cudaMemcpyAsync(b->pool_u2, su2, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    cudaMemcpyAsync(b->ctls, sctl, sizeof(Ctl) * (size_t)b->nprob, cudaMemcpyDeviceToDevice, b->stream);
+    b->cur_slot = slot_saved;
+    b->folded = folded_saved;
+  };
+  float best = 1e30f;
+  int bv = b->variant, bm = b->mult, bo = b->order;
+  int rc = E2D_OK;
+  for (int v = 0; v <= 1 && rc == E2D_OK; ++v)
+    for (int m : {1, 2, 4})
+      for (int o = 0; o <= 1 && rc == E2D_OK; ++o) {
+        if ((rc = e2d_batch_set_schedule(b, v, m, o))) break;
+        float ms = 0;
+        for (int rep = 0; rep < 2 && rc == E2D_OK; ++rep) {  // the first pass captures the graph
+          restore();
+          if ((rc = advance_impl(b, 0, steps, nullptr))) break;
+          rc = e2d_batch_last_advance_ms(b, &ms);
+        }
+        if (rc == E2D_OK && ms < best) {
+          best = ms;
+          bv = v;
+          bm = m;
+          bo = o;
+        }
+      }
+  restore();
+  cudaStreamSynchronize(b->stream);
+  cudaFree(su);
+  cudaFree(su2);
+  cudaFree(sctl);
+  if (rc) return rc;
+  if (best_ms) *best_ms = best;
+  if (cache_path) {
+    std::ofstream outf(cache_path, std::ios::app);
+    outf << sig << " " << bv << " " << bm << " " << bo << " " << best << "\n";
+  }
+  return e2d_batch_set_schedule(b, bv, bm, bo);
+}
+
+int e2d_batch_get_health(e2d_batch* b, int prob, unsigned* flags) {
+  if (int rc = check(b)) return rc;
+  if (prob < 0 || prob >= b->nprob || !flags) return bfail(E2D_ERR_INVALID_ARG, "bad health arguments");
+  B_CK(cudaStreamSynchronize(b->stream));
+  B_CK(cudaMemcpy(flags, &b->ctls[prob].health, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  return E2D_OK;
+}
+
+}  // extern "C"

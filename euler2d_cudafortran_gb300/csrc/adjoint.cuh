@@ -1,0 +1,258 @@
+// adjoint.cuh -- hand-written reverse (adjoint) versions of the pointwise
+// routines of physics.cuh, for the discrete adjoint of the FP64 step.
+//
+// Each *_rev routine recomputes what it needs of its forward routine (same
+// operations, same branch decisions: limiter case, max/min selections, HLLC
+// sampling branch, density and pressure floors) and accumulates the
+// transposed Jacobian applied to the output adjoint into the input adjoints
+// ("+=" semantics).  Ties in max/min follow the forward selection of Ops
+// (the second argument wins a tie), so the derivative is a consistent
+// one-sided derivative at those points.  Supported: the HLLC flux (the
+// two-shock solver's Newton loop has no adjoint here).
+#pragma once
+#include "physics.cuh"
+
+namespace e2d {
+namespace adj {
+
+using O = Ops<double>;
+
+__device__ __forceinline__ bool picks_first_max(double a, double b) { return emul::gt_i(a, b); }  // max(a,b) == a
+__device__ __forceinline__ bool picks_first_min(double a, double b) { return emul::ord(a) < emul::ord(b); }
+
+// computePrimitives (serial_ref/m_utils.f90:35-64) reverse: qb (adjoint of
+// r, p, u, v) -> ub (adjoint of rho, E, rho u, rho v).
+__device__ __forceinline__ void primitives_rev(const Hydro<double>& h, const double u[4], const double qb[4],
+                                               double ub[4]) {
+  const double r = O::max(u[ID], h.smallr);
+  const double uu = O::div(u[IU], r), vv = O::div(u[IV], r);
+  const double eken = O::half(uu * uu + vv * vv);
+  const double eu = O::div(u[IP], r);
+  const double e = eu - eken;
+  const double pa = (h.gm1 * r) * e, pb = r * h.smallp;
+  double rb = qb[ID], eb = 0.0;
+  if (picks_first_max(pa, pb)) {
+    rb += qb[IP] * h.gm1 * e;
+    eb = qb[IP] * h.gm1 * r;
+  } else {
+    rb += qb[IP] * h.smallp;
+  }
+  // e = E/r - 0.5 (u^2 + v^2)
+  double ubu = qb[IU] - eb * uu;
+  double ubv = qb[IV] - eb * vv;
+  ub[IP] += O::div(eb, r);
+  rb -= O::div(eb * eu, r);
+  // u = (rho u)/r, v = (rho v)/r
+  ub[IU] += O::div(ubu, r);
+  ub[IV] += O::div(ubv, r);
+  rb -= O::div(ubu * uu + ubv * vv, r);
+  if (picks_first_max(u[ID], h.smallr)) ub[ID] += rb;
+}
+
+// The compute_dt term of one cell (serial_ref/m_run.f90:278-281) reverse.
+__device__ __forceinline__ void cell_invdt_rev(const Hydro<double>& h, const double u[4], double tb, double ub[4]) {
+  double q[4];
+  primitives(h, u, q);
+  const double c2 = O::div(h.gamma0 * q[IP], q[ID]);
+  const double c = O::sqrt(c2);
+  double qb[4] = {0.0, 0.0, 0.0, 0.0};
+  const double cb = O::div(tb, h.dx) + O::div(tb, h.dy);
+  qb[IU] = O::neg_if(O::div(tb, h.dx), !O::ge0(q[IU]));
+  qb[IV] = O::neg_if(O::div(tb, h.dy), !O::ge0(q[IV]));
+  const double c2b = O::div(cb, 2.0 * c);
+  qb[IP] += O::div(c2b * h.gamma0, q[ID]);
+  qb[ID] -= O::div(c2b * c2, q[ID]);
+  primitives_rev(h, u, qb, ub);
+}
+
+// One slope (slope_unsplit_hydro_2d, one variable and direction) reverse:
+// adds d(slope)/d(q, qp, qm) * sb.
+__device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double qm, double sb, double& qbar,
+                                           double& qpbar, double& qmbar) {
+  const double dl = q - qm, dr = qp - q;
+  const double dlft = mc ? O::twice(dl) : dl;
+  const double drgt = mc ? O::twice(dr) : dr;
+  const double dcen = O::half(qp - qm);
+  if (O::le0(dlft * drgt)) return;  // limited to zero
+  const double st = mc ? 2.0 : 1.0;
+  const bool neg = !O::ge0(dcen);   // dsgn = -1
+  const double al = fabs(dlft), ar = fabs(drgt), ac = fabs(dcen);
+  const bool use_l = picks_first_min(al, ar);
+  const double slop = use_l ? al : ar;
+  if (picks_first_min(slop, ac)) {
+    // slope = dsgn * |dlft| or dsgn * |drgt|
+    const double x = use_l ? dlft : drgt;
+    const double g = ((!O::ge0(x)) != neg) ? -sb : sb;  // dsgn * sign(x) * sb
+    if (use_l) { qbar += st * g; qmbar -= st * g; }
+    else { qpbar += st * g; qbar -= st * g; }
+  } else {
+    // slope = dsgn * |dcen| = dcen
+    const double g = ((!O::ge0(dcen)) != neg) ? -sb : sb;
+    qpbar += 0.5 * g;
+    qmbar -= 0.5 * g;
+  }
+}
+
+// trace_sources reverse: sb -> (qb, dqxb, dqyb).
+__device__ __forceinline__ void trace_sources_rev(const Hydro<double>& h, const double q[4], const double dqx[4],
+                                                  const double dqy[4], const double sb[4], double qb[4],
+                                                  double dqxb[4], double dqyb[4]) {
+  const double r = q[ID], p = q[IP], u = q[IU], v = q[IV];
+  const double div_ = dqx[IU] + dqy[IV];
+  qb[IU] -= sb[ID] * dqx[ID] + sb[IP] * dqx[IP] + sb[IU] * dqx[IU] + sb[IV] * dqx[IV];
+  qb[IV] -= sb[ID] * dqy[ID] + sb[IP] * dqy[IP] + sb[IU] * dqy[IU] + sb[IV] * dqy[IV];
+  qb[ID] -= sb[ID] * div_;
+  qb[ID] += O::div(O::div(sb[IU] * dqx[IP] + sb[IV] * dqy[IP], r), r);
+  qb[IP] -= sb[IP] * div_ * h.gamma0;
+  dqxb[ID] -= sb[ID] * u;
+  dqyb[ID] -= sb[ID] * v;
+  dqxb[IP] -= sb[IP] * u + O::div(sb[IU], r);
+  dqyb[IP] -= sb[IP] * v + O::div(sb[IV], r);
+  const double dd = sb[ID] * r + sb[IP] * h.gamma0 * p;
+  dqxb[IU] -= dd + sb[IU] * u;
+  dqyb[IU] -= sb[IU] * v;
+  dqxb[IV] -= sb[IV] * u;
+  dqyb[IV] -= dd + sb[IV] * v;
+}
+
+// trace_face reverse: qfb -> (qb, dqb, sb) and the dt/d adjoint dtdb.
+template <bool PLUS>
+__device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const double q[4], const double dq[4],
+                                               const double s[4], double dtd, const double qfb_in[4],
+                                               double qb[4], double dqb[4], double sb[4], double& dtdb) {
+  double qfb[4] = {qfb_in[0], qfb_in[1], qfb_in[2], qfb_in[3]};
+  const double a = PLUS ? (q[ID] + O::half(dq[ID])) : (q[ID] - O::half(dq[ID]));
+  const double raw = a + O::half(s[ID] * dtd);
+  // max(smallr, raw) returns raw unless smallr > raw: no gradient through the floor
+  if (emul::gt_i(h.smallr, raw)) qfb[ID] = 0.0;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    qb[v] += qfb[v];
+    dqb[v] += PLUS ? 0.5 * qfb[v] : -0.5 * qfb[v];
+    sb[v] += 0.5 * dtd * qfb[v];
+    dtdb += 0.5 * s[v] * qfb[v];
+  }
+}
+
+// riemann_2d_hllc (serial_ref/m_utils.f90:534-644) reverse: fb -> (qlb, qrb).
+__device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const double ql[4], const double qr[4],
+                                                 const double fb[4], double qlb[4], double qrb[4]) {
+  // ---- forward recomputation (same operations and branches as riemann_hllc)
+  const double rl = O::max(ql[ID], h.smallr), rr = O::max(qr[ID], h.smallr);
+  const double rlsp = rl * h.smallp, rrsp = rr * h.smallp;
+  const double pl = O::max(ql[IP], rlsp), pr = O::max(qr[IP], rrsp);
+  const double ul = ql[IU], ur = qr[IU], vl = ql[IV], vr = qr[IV];
+  const double hrl = O::half(rl), hrr = O::half(rr);
+  const double etotl = (pl * h.entho) + (((hrl * ul) * ul) + ((hrl * vl) * vl));
+  const double etotr = (pr * h.entho) + (((hrr * ur) * ur) + ((hrr * vr) * vr));
+  const double cal = O::div(h.gamma0 * pl, rl), car = O::div(h.gamma0 * pr, rr);
+  const bool cl_act = picks_first_max(cal, h.smallc2), cr_act = picks_first_max(car, h.smallc2);
+  const double cfastl = O::sqrt(cl_act ? cal : h.smallc2), cfastr = O::sqrt(cr_act ? car : h.smallc2);
+  const bool cmax_l = picks_first_max(cfastl, cfastr);
+  const double cmax = cmax_l ? cfastl : cfastr;
+  const bool min_l = picks_first_min(ul, ur), max_l = picks_first_max(ul, ur);
+  const double SL = (min_l ? ul : ur) - cmax;
+  const double SR = (max_l ? ul : ur) + cmax;
+  const double rcl = rl * (ul - SL), rcr = rr * (SR - ur);
+  const double den = rcr + rcl;
+  const double ustar = O::div(((rcr * ur) + (rcl * ul)) + (pl - pr), den);
+  const double ptotstar = O::div(((rcr * pl) + (rcl * pr)) + ((rcl * rcr) * (ul - ur)), den);
+  int branch;
+  double ro, uo, ptoto, etoto, d = 1.0, nE = 0.0;
+  if (O::gt0(SL)) { branch = 1; ro = rl; uo = ul; ptoto = pl; etoto = etotl; }
+  else if (O::gt0(ustar)) {
+    branch = 2; d = SL - ustar;
+    ro = O::div(rl * (SL - ul), d); uo = ustar; ptoto = ptotstar;
+    nE = (((SL - ul) * etotl) - (pl * ul)) + (ptotstar * ustar); etoto = O::div(nE, d);
+  } else if (O::gt0(SR)) {
+    branch = 3; d = SR - ustar;
+    ro = O::div(rr * (SR - ur), d); uo = ustar; ptoto = ptotstar;
+    nE = (((SR - ur) * etotr) - (pr * ur)) + (ptotstar * ustar); etoto = O::div(nE, d);
+  } else { branch = 4; ro = rr; uo = ur; ptoto = pr; etoto = etotr; }
+  const double fr = ro * uo;
+  const bool vleft = O::gt0(fr);
+
+  // ---- reverse
+  double rlb = 0, rrb = 0, plb = 0, prb = 0, ulb = 0, urb = 0, vlb = 0, vrb = 0, etotlb = 0, etotrb = 0;
+  double SLb = 0, SRb = 0, ustarb = 0, ptotstarb = 0;
+  // flux[IV] = fr * (vl or vr)
+  double frb = fb[ID] + fb[IV] * (vleft ? vl : vr);
+  if (vleft) vlb += fb[IV] * fr; else vrb += fb[IV] * fr;
+  // flux[IU] = fr * uo + ptoto ; flux[IP] = (etoto + ptoto) * uo
+  double uob = fb[IU] * fr + fb[IP] * (etoto + ptoto);
+  frb += fb[IU] * uo;
+  double ptotob = fb[IU] + fb[IP] * uo;
+  double etotob = fb[IP] * uo;
+  // fr = ro * uo
+  double rob = frb * uo;
+  uob += frb * ro;
+  switch (branch) {
+    case 1: rlb += rob; ulb += uob; plb += ptotob; etotlb += etotob; break;
+    case 4: rrb += rob; urb += uob; prb += ptotob; etotrb += etotob; break;
+    case 2: {
+      ustarb += uob; ptotstarb += ptotob;
+      double db = -O::div(rob * ro, d) - O::div(etotob * etoto, d);
+      const double rq = O::div(rob, d);
+      rlb += rq * (SL - ul); SLb += rq * rl; ulb -= rq * rl;
+      const double nEb = O::div(etotob, d);
+      SLb += nEb * etotl; ulb -= nEb * etotl; etotlb += nEb * (SL - ul);
+      plb -= nEb * ul; ulb -= nEb * pl; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
+      SLb += db; ustarb -= db;
+      break;
+    }
+    default: {  // 3
+      ustarb += uob; ptotstarb += ptotob;
+      double db = -O::div(rob * ro, d) - O::div(etotob * etoto, d);
+      const double rq = O::div(rob, d);
+      rrb += rq * (SR - ur); SRb += rq * rr; urb -= rq * rr;
+      const double nEb = O::div(etotob, d);
+      SRb += nEb * etotr; urb -= nEb * etotr; etotrb += nEb * (SR - ur);
+      prb -= nEb * ur; urb -= nEb * pr; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
+      SRb += db; ustarb -= db;
+      break;
+    }
+  }
+  // ptotstar and ustar = num / den
+  const double npb = O::div(ptotstarb, den), nub = O::div(ustarb, den);
+  double denb = -npb * ptotstar - nub * ustar;
+  double rcrb = npb * (pl + rcl * (ul - ur)) + nub * ur + denb;
+  double rclb = npb * (pr + rcr * (ul - ur)) + nub * ul + denb;
+  plb += npb * rcr + nub;
+  prb += npb * rcl - nub;
+  ulb += npb * rcl * rcr + nub * rcl;
+  urb += -npb * rcl * rcr + nub * rcr;
+  // rcr = rr (SR - ur), rcl = rl (ul - SL)
+  rrb += rcrb * (SR - ur); SRb += rcrb * rr; urb -= rcrb * rr;
+  rlb += rclb * (ul - SL); ulb += rclb * rl; SLb -= rclb * rl;
+  // SR = max(ul, ur) + cmax, SL = min(ul, ur) - cmax
+  const double cmaxb = SRb - SLb;
+  if (max_l) ulb += SRb; else urb += SRb;
+  if (min_l) ulb += SLb; else urb += SLb;
+  const double cfastlb = cmax_l ? cmaxb : 0.0, cfastrb = cmax_l ? 0.0 : cmaxb;
+  if (cl_act) {
+    const double cab = O::div(cfastlb, 2.0 * cfastl);
+    plb += O::div(cab * h.gamma0, rl);
+    rlb -= O::div(cab * cal, rl);
+  }
+  if (cr_act) {
+    const double cab = O::div(cfastrb, 2.0 * cfastr);
+    prb += O::div(cab * h.gamma0, rr);
+    rrb -= O::div(cab * car, rr);
+  }
+  // etot = p entho + hr u u + hr v v, hr = rho / 2
+  plb += etotlb * h.entho; prb += etotrb * h.entho;
+  rlb += 0.5 * etotlb * (ul * ul + vl * vl);
+  rrb += 0.5 * etotrb * (ur * ur + vr * vr);
+  ulb += etotlb * 2.0 * hrl * ul; vlb += etotlb * 2.0 * hrl * vl;
+  urb += etotrb * 2.0 * hrr * ur; vrb += etotrb * 2.0 * hrr * vr;
+  // pressure and density floors
+  if (picks_first_max(ql[IP], rlsp)) qlb[IP] += plb; else rlb += plb * h.smallp;
+  if (picks_first_max(qr[IP], rrsp)) qrb[IP] += prb; else rrb += prb * h.smallp;
+  if (picks_first_max(ql[ID], h.smallr)) qlb[ID] += rlb;
+  if (picks_first_max(qr[ID], h.smallr)) qrb[ID] += rrb;
+  qlb[IU] += ulb; qlb[IV] += vlb;
+  qrb[IU] += urb; qrb[IV] += vrb;
+}
+
+}  // namespace adj
+}  // namespace e2d

@@ -1,0 +1,34 @@
+// batch.h -- device-side description of an ensemble of independent runs.
+#pragma once
+#include "launch.h"
+
+namespace e2d {
+
+template <typename Real>
+struct BatchProb {
+  Hydro<Real> h;   // this problem's parameters (size, boundaries, constants)
+  Real* u;         // pitched states, as a single run's u and u2
+  Real* u2;
+  int pitch;
+  long long plane;
+  int ntx, nty;    // tiles of the chosen shape
+  int tile_begin;  // first index of this problem in the flattened tile list
+  int id;          // problem index (its control block and dt-log column)
+};
+
+template <typename Real>
+struct BatchLaunch {
+  const BatchProb<Real>* probs;  // device array, in work-list order
+  int nprob, total_tiles, parity, rd, wr, grid;
+  Ctl* ctls;      // per-problem running CFL maxima and health flags, by problem index
+  Real* dt_log;   // device, nprob entries for this step by problem index (may be null)
+  const Real* dt_src = nullptr;  // if set: step with these logged dt (by problem index), no CFL fold
+  Real* inv_log = nullptr;       // if set: receives each problem's running CFL maximum before the step
+};
+
+// Tile shapes: variant 0 = 32 x 15 cells (256 threads), 1 = 32 x 7 (128 threads).
+template <typename Real> int batch_tile_shape(int variant, int* tx, int* ty, int* nt);
+template <typename Real> int batch_resident_per_sm(int variant);
+template <typename Real> void launch_batch_step(int variant, const BatchLaunch<Real>& L, cudaStream_t s);
+
+}  // namespace e2d

@@ -1,0 +1,593 @@
+// k_adjoint.cu -- reverse (adjoint) kernels of the FP64 step.
+//
+// k_step_rev: given the state U_n (ghosts filled) and the adjoint of the next
+// state Ubar_{n+1} (interior cells), accumulates Ubar_n and the adjoint of the
+// step's dt.  A CTA owns a 32 x 7 tile; it recomputes the forward values of
+// its box (primitives, slopes, trace sources), then for each face it owns
+// (the left / lower faces of its cells, plus the last wall faces) forms the
+// flux adjoint from the update (F_i enters cell i with + and cell i-1 with -),
+// runs the Riemann, trace, source, slope and primitive reverses, and scatters
+// the result into shared accumulators; ghost-cell adjoints are folded back to
+// the interior cells make_boundaries copied them from (serial_ref/m_run.f90:
+// 561-648).  The 2x2 ghost corners are constants and receive nothing.
+#include "adjoint.cuh"
+#include "adjoint_launch.h"
+#include "tile.cuh"
+
+namespace e2d {
+
+namespace {
+
+constexpr int ATX = 32, ATY = 7, ANT = 128;
+constexpr int ABX = ATX + 4, ABY = ATY + 4, ARX = ATX + 2, ARY = ATY + 2;
+constexpr int NBOX = ABX * ABY, NRING = ARX * ARY;
+constexpr int NUB = (ATX + 1) * (ATY + 1);
+// shared layout (doubles)
+constexpr int Q_OFF = 0;                        // q box      [4][ABY][ABX]
+constexpr int DQ_OFF = Q_OFF + 4 * NBOX;        // slopes     [8][ARY][ARX]
+constexpr int S_OFF = DQ_OFF + 8 * NRING;       // sources    [4][ARY][ARX]
+constexpr int UB_OFF = S_OFF + 4 * NRING;       // Ubar'      [4][ATY+1][ATX+1], cells (i0-1.., j0-1..)
+constexpr int RA_OFF = UB_OFF + 4 * NUB;        // ring adj.  dqx[4] dqy[4] s[4]: [12][ARY][ARX]
+constexpr int QB_OFF = RA_OFF + 12 * NRING;     // q adjoint  [4][ABY][ABX]
+constexpr int N_SMEM = QB_OFF + 4 * NBOX;
+constexpr size_t SMEM_BYTES = (size_t)N_SMEM * sizeof(double) + 64;
+
+__device__ __forceinline__ void sadd(double* p, double x) {
+  if (x != 0.0) atomicAdd(p, x);
+}
+
+// One 32 x 7 tile (bx, by) of the reverse step; sm is the dynamic shared area.
+__device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
+                                              Field<double> ubn, double dt, double* dtbar, int bx, int by,
+                                              double* sm) {
+  double* sq = sm + Q_OFF;
+  double* sdq = sm + DQ_OFF;
+  double* ss = sm + S_OFF;
+  double* sub = sm + UB_OFF;
+  double* sra = sm + RA_OFF;
+  double* sqb = sm + QB_OFF;
+  __shared__ double red[2][ANT / 32];
+  const int tid = threadIdx.x;
+  const int i0 = GW + bx * ATX, j0 = GW + by * ATY;
+  const double dtdx = dt / h.dx, dtdy = dt / h.dy;
+
+  // ---- load U box, Ubar' of cells [i0-1, i0+ATX) x [j0-1, j0+ATY), zero accumulators
+  for (int k = tid; k < 4 * NBOX; k += ANT) {
+    const int v = k / NBOX, rem = k - v * NBOX, y = rem / ABX, x = rem - y * ABX;
+    const int gi = i0 - GW + x, gj = j0 - GW + y;
+    sq[k] = (gi < h.isize && gj < h.jsize) ? un.at(v, gj, gi) : 0.0;
+    sqb[k] = 0.0;
+  }
+  for (int k = tid; k < 12 * NRING; k += ANT) sra[k] = 0.0;
+  for (int k = tid; k < 4 * NUB; k += ANT) {
+    const int v = k / NUB, rem = k - v * NUB, y = rem / (ATX + 1), x = rem - y * (ATX + 1);
+    const int gi = i0 - 1 + x, gj = j0 - 1 + y;
+    const bool interior = gi >= GW && gi <= h.nx + 1 && gj >= GW && gj <= h.ny + 1;
+    sub[k] = interior ? ubn1.at(v, gj, gi) : 0.0;
+  }
+  __syncthreads();
+  // ---- forward recomputation: primitives (box), slopes and sources (ring)
+  for (int k = tid; k < NBOX; k += ANT) {
+    double u[4], q[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) u[v] = sq[v * NBOX + k];
+    primitives(h, u, q);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sq[v * NBOX + k] = q[v];
+  }
+  __syncthreads();
+  auto Q = [&](int v, int y, int x) -> double { return sq[(v * ABY + y) * ABX + x]; };
+  for (int k = tid; k < NRING; k += ANT) {
+    const int x = k % ARX + 1, y = k / ARX + 1;
+    double qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qc[v] = Q(v, y, x); qe[v] = Q(v, y, x + 1); qw[v] = Q(v, y, x - 1);
+      qn[v] = Q(v, y + 1, x); qs[v] = Q(v, y - 1, x);
+    }
+    slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
+    trace_sources(h, qc, dqx, dqy, s);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      sdq[v * NRING + k] = dqx[v];
+      sdq[(4 + v) * NRING + k] = dqy[v];
+      ss[v * NRING + k] = s[v];
+    }
+  }
+  __syncthreads();
+
+  // ---- owned faces: flux adjoint -> Riemann, trace reverse
+  double dtdxb = 0.0, dtdyb = 0.0;
+  auto UB = [&](int v, int i, int j) -> double {  // Ubar' of absolute cell (i, j), zero outside the interior
+    const int x = i - (i0 - 1), y = j - (j0 - 1);
+    return (x >= 0 && x <= ATX && y >= 0 && y <= ATY) ? sub[(v * (ATY + 1) + y) * (ATX + 1) + x] : 0.0;
+  };
+  constexpr int NXF = (ATX + 1) * ATY, NYF = ATX * (ATY + 1);
+  for (int k = tid; k < NXF + NYF; k += ANT) {
+    const bool xface = k < NXF;
+    int a, b;  // ring indices of the two cells (left/lower, right/upper)
+    int ia, ja;
+    double fb[4];
+    if (xface) {
+      const int f = k % (ATX + 1), r = k / (ATX + 1);
+      const int i = i0 + f, j = j0 + r;
+      if (!(i <= h.nx + 2 && j <= h.ny + 1 && (f < ATX || i == h.nx + 2))) continue;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fb[v] = UB(v, i, j) - UB(v, i - 1, j);
+      a = (r + 1) * ARX + f;
+      b = a + 1;
+      ia = f + 1; ja = r + 2;  // box coordinates of the left cell
+    } else {
+      const int kk = k - NXF;
+      const int c = kk % ATX, g = kk / ATX;
+      const int i = i0 + c, j = j0 + g;
+      if (!(i <= h.nx + 1 && j <= h.ny + 2 && (g < ATY || j == h.ny + 2))) continue;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fb[v] = UB(v, i, j) - UB(v, i, j - 1);
+      a = g * ARX + (c + 1);
+      b = a + ARX;
+      ia = c + 2; ja = g + 1;  // box coordinates of the lower cell
+    }
+    const double dtd = xface ? dtdx : dtdy;
+    const int nrm = xface ? 0 : 4;  // slope block of the face normal
+    double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], ql[4], qr[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qa[v] = Q(v, ja, ia);
+      qb_[v] = xface ? Q(v, ja, ia + 1) : Q(v, ja + 1, ia);
+      dqa[v] = sdq[(nrm + v) * NRING + a]; dqb[v] = sdq[(nrm + v) * NRING + b];
+      sa[v] = ss[v * NRING + a]; sb[v] = ss[v * NRING + b];
+    }
+    trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
+    trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
+    if (!xface) {
+      double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
+      t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
+    }
+    double flux[4];
+    riemann_hllc(h, ql, qr, flux);
+    double rb[4];
+    if (xface) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { dtdxb += flux[v] * fb[v]; rb[v] = fb[v] * dtd; }
+    } else {  // the stored y flux is the Riemann flux with IU and IV swapped back
+      dtdyb += flux[ID] * fb[ID] + flux[IP] * fb[IP] + flux[IV] * fb[IU] + flux[IU] * fb[IV];
+      rb[ID] = fb[ID] * dtd; rb[IP] = fb[IP] * dtd; rb[IU] = fb[IV] * dtd; rb[IV] = fb[IU] * dtd;
+    }
+    double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0};
+    adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb);
+    if (!xface) {
+      double t = qlb[IU]; qlb[IU] = qlb[IV]; qlb[IV] = t;
+      t = qrb[IU]; qrb[IU] = qrb[IV]; qrb[IV] = t;
+    }
+    double qab[4] = {0, 0, 0, 0}, dqab[4] = {0, 0, 0, 0}, sab[4] = {0, 0, 0, 0};
+    double qbb[4] = {0, 0, 0, 0}, dqbb[4] = {0, 0, 0, 0}, sbb[4] = {0, 0, 0, 0};
+    double& dtdb = xface ? dtdxb : dtdyb;
+    adj::trace_face_rev<true>(h, qa, dqa, sa, dtd, qlb, qab, dqab, sab, dtdb);
+    adj::trace_face_rev<false>(h, qb_, dqb, sb, dtd, qrb, qbb, dqbb, sbb, dtdb);
+    const int ka = ja * ABX + ia;
+    const int kb = xface ? ka + 1 : ka + ABX;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      sadd(&sqb[v * NBOX + ka], qab[v]);
+      sadd(&sqb[v * NBOX + kb], qbb[v]);
+      sadd(&sra[(nrm + v) * NRING + a], dqab[v]);
+      sadd(&sra[(nrm + v) * NRING + b], dqbb[v]);
+      sadd(&sra[(8 + v) * NRING + a], sab[v]);
+      sadd(&sra[(8 + v) * NRING + b], sbb[v]);
+    }
+  }
+  __syncthreads();
+
+  // ---- ring cells: sources and slopes reverse
+  const bool mc = h.slope_type == 2;
+  const bool lim = h.slope_type == 1 || h.slope_type == 2;
+  for (int k = tid; k < NRING; k += ANT) {
+    const int x = k % ARX + 1, y = k / ARX + 1;
+    double qc[4], dqx[4], dqy[4], sbar[4], dqxb[4], dqyb[4], qcb[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qc[v] = Q(v, y, x);
+      dqx[v] = sdq[v * NRING + k]; dqy[v] = sdq[(4 + v) * NRING + k];
+      dqxb[v] = sra[v * NRING + k]; dqyb[v] = sra[(4 + v) * NRING + k];
+      sbar[v] = sra[(8 + v) * NRING + k];
+    }
+    adj::trace_sources_rev(h, qc, dqx, dqy, sbar, qcb, dqxb, dqyb);
+    const int kc = y * ABX + x;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double qe = 0, qw = 0, qn = 0, qs = 0;
+      if (lim) {
+        adj::slope1_rev(mc, qc[v], Q(v, y, x + 1), Q(v, y, x - 1), dqxb[v], qcb[v], qe, qw);
+        adj::slope1_rev(mc, qc[v], Q(v, y + 1, x), Q(v, y - 1, x), dqyb[v], qcb[v], qn, qs);
+      }
+      sadd(&sqb[v * NBOX + kc], qcb[v]);
+      sadd(&sqb[v * NBOX + kc + 1], qe);
+      sadd(&sqb[v * NBOX + kc - 1], qw);
+      sadd(&sqb[v * NBOX + kc + ABX], qn);
+      sadd(&sqb[v * NBOX + kc - ABX], qs);
+    }
+  }
+  __syncthreads();
+
+  // ---- box cells: primitives reverse, fold ghosts back, identity part of the update
+  for (int k = tid; k < NBOX; k += ANT) {
+    const int y = k / ABX, x = k - y * ABX;
+    const int gi = i0 - GW + x, gj = j0 - GW + y;
+    if (gi >= h.isize || gj >= h.jsize) continue;
+    const bool xin = gi >= GW && gi <= h.nx + 1, yin = gj >= GW && gj <= h.ny + 1;
+    if (!xin && !yin) continue;  // corner: a constant
+    double qb[4], u[4], ub[4] = {0, 0, 0, 0};
+    bool any = false;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) { qb[v] = sqb[v * NBOX + k]; any |= qb[v] != 0.0; }
+    if (any) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) u[v] = un.at(v, gj, gi);
+      adj::primitives_rev(h, u, qb, ub);
+    }
+    if (xin && yin) {
+      // own interior cells of this tile also carry Ubar' through U' = U + ...
+      if (gi >= i0 && gi < i0 + ATX && gj >= j0 && gj < j0 + ATY) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) ub[v] += UB(v, gi, gj);
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) if (ub[v] != 0.0) atomicAdd(&ubn.at(v, gj, gi), ub[v]);
+    } else if (any) {
+      int si = gi, sj = gj, type, flip;
+      if (!xin) {
+        type = gi < GW ? h.bc_xmin : h.bc_xmax;
+        si = ghost_source(gi, h.nx, type);
+        flip = IU;
+      } else {
+        type = gj < GW ? h.bc_ymin : h.bc_ymax;
+        sj = ghost_source(gj, h.ny, type);
+        flip = IV;
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double g = (type == 1 && v == flip) ? -ub[v] : ub[v];
+        if (g != 0.0) atomicAdd(&ubn.at(v, sj, si), g);
+      }
+    }
+  }
+  // ---- dt adjoint: dtdx = dt/dx, dtdy = dt/dy
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dtdxb += __shfl_xor_sync(0xffffffffu, dtdxb, o);
+    dtdyb += __shfl_xor_sync(0xffffffffu, dtdyb, o);
+  }
+  if ((tid & 31) == 0) { red[0][tid >> 5] = dtdxb; red[1][tid >> 5] = dtdyb; }
+  __syncthreads();
+  if (tid == 0) {
+    double sx = 0, sy = 0;
+    for (int w = 0; w < ANT / 32; ++w) { sx += red[0][w]; sy += red[1][w]; }
+    atomicAdd(dtbar, sx / h.dx + sy / h.dy);
+  }
+}
+
+__global__ void __launch_bounds__(ANT, 2)
+    k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, const double* dt,
+               double* dtbar) {
+  extern __shared__ double sm[];
+  step_rev_tile(h, un, ubn1, ubn, *dt, dtbar, blockIdx.x, blockIdx.y, sm);
+}
+
+// The 2x2 ghost corners are never written by a step, so a state keeps the
+// corners of the buffer it lands in: the initial state's in u (even steps),
+// zeros in u2 (odd steps).  Segment buffer j = 1..nseg-1 (state k0 + j)
+// receives the corners of ping-pong buffer (k0 + j) & 1 before recomputation.
+// 64 threads: var (4) x corner (4) x 2 x 2.
+__device__ __forceinline__ void copy_corner(const double* src, double* dst, int pitch, long long plane, int isize,
+                                            int jsize, int t) {
+  const int v = t >> 4, c = (t >> 2) & 3, dy = (t >> 1) & 1, dx = t & 1;
+  const int i = (c & 1) ? isize - 2 + dx : dx, jj = (c & 2) ? jsize - 2 + dy : dy;
+  const long long o = v * plane + (long long)jj * pitch + i;
+  dst[o] = src[o];
+}
+
+__global__ void k_seg_corners(double* pool, long long state_elems, int pitch, long long plane, int isize, int jsize,
+                              int ping_index, int seg_index, int k0) {
+  const int j = blockIdx.x + 1;
+  if (threadIdx.x >= 64) return;
+  copy_corner(pool + (long long)(ping_index + ((k0 + j) & 1)) * state_elems,
+              pool + (long long)(seg_index + j) * state_elems, pitch, plane, isize, jsize, threadIdx.x);
+}
+
+// Does the running CFL maximum rise at state m?  (The maxima are logged with
+// stride `stride`: one entry per problem and step.)
+__device__ __forceinline__ bool max_rises(const double* inv_log, int m, int stride) {
+  return m == 0 || inv_log[(long long)m * stride] > inv_log[(long long)(m - 1) * stride];
+}
+
+// Largest compute_dt term of a state and the cell (i + j*isize) that has it;
+// on equal terms the lowest index wins.  CTA `part` of `nparts` takes every
+// nparts-th row; 256 threads.
+__device__ __forceinline__ void argmax_part(const Hydro<double>& h, Field<double> u, int part, int nparts, double* pv,
+                                            long long* pi) {
+  double best = -1.0;
+  long long bi = 0x7fffffffffffffffll;
+  for (int j = GW + part; j <= h.jsize - 4; j += nparts)
+    for (int i = GW + threadIdx.x; i <= h.isize - 4; i += blockDim.x) {
+      double uc[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) uc[v] = u.at(v, j, i);
+      const double t = cell_invdt(h, uc);
+      const long long idx = (long long)j * h.isize + i;
+      if (t > best || (t == best && idx < bi)) { best = t; bi = idx; }
+    }
+  __shared__ double sv[256];
+  __shared__ long long si[256];
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const double v2 = sv[threadIdx.x + s];
+      const long long i2 = si[threadIdx.x + s];
+      if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
+        sv[threadIdx.x] = v2;
+        si[threadIdx.x] = i2;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { pv[part] = sv[0]; pi[part] = si[0]; }
+}
+
+// If the running maximum rises at state m, the steps [m, n1) up to the next
+// rise use the compute_dt term of the argmax cell of state m; their dt
+// adjoints go to Ubar_m: dt_n = cfl / inv_n, d dt_n / d inv_n = -cfl / inv_n^2.
+// One thread; logs have stride `stride`.
+__device__ __forceinline__ void dt_route(const Hydro<double>& h, Field<double> u, Field<double> ub, const double* pv,
+                                         const long long* pi, int nparts, const double* dtbar_log,
+                                         const double* inv_log, int stride, int m, int nsteps) {
+  int n1 = m + 1;
+  while (n1 < nsteps && !max_rises(inv_log, n1, stride)) ++n1;
+  double best = -1.0;
+  long long bi = 0x7fffffffffffffffll;
+  for (int k = 0; k < nparts; ++k)
+    if (pv[k] > best || (pv[k] == best && pi[k] < bi)) { best = pv[k]; bi = pi[k]; }
+  double s = 0.0;
+  for (int n = m; n < n1; ++n) {
+    const double inv = inv_log[(long long)n * stride];
+    s += -h.cfl / (inv * inv) * dtbar_log[(long long)n * stride];
+  }
+  const int j = (int)(bi / h.isize), i = (int)(bi - (long long)j * h.isize);
+  double uc[4], g[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int v = 0; v < 4; ++v) uc[v] = u.at(v, j, i);
+  adj::cell_invdt_rev(h, uc, s, g);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) ub.at(v, j, i) += g[v];
+}
+
+__global__ void k_argmax_partial(Hydro<double> h, Field<double> u, double* pv, long long* pi, const double* inv_log,
+                                 int m) {
+  if (!max_rises(inv_log, m, 1)) return;  // only states where the running maximum rises
+  argmax_part(h, u, blockIdx.x, gridDim.x, pv, pi);
+}
+
+__global__ void k_dt_route(Hydro<double> h, Field<double> u, Field<double> ub, const double* pv,
+                           const long long* pi, int nparts, const double* dtbar_log, const double* inv_log, int m,
+                           int nsteps) {
+  if (threadIdx.x != 0 || blockIdx.x != 0 || !max_rises(inv_log, m, 1)) return;
+  dt_route(h, u, ub, pv, pi, nparts, dtbar_log, inv_log, 1, m, nsteps);
+}
+
+// J = sum over interior cells of rho^2 w(x, y), w a Gaussian of width sigma
+// centred at (xc, yc), cell centres x = (i - 2 + 1/2) dx; and dJ/dU.
+__device__ __forceinline__ double weight(const Hydro<double>& h, int i, int j, double xc, double yc, double sig) {
+  const double x = (i - GW + 0.5) * h.dx, y = (j - GW + 0.5) * h.dy;
+  return exp(-((x - xc) * (x - xc) + (y - yc) * (y - yc)) / (2.0 * sig * sig));
+}
+
+// Grid-stride over the interior with `nthreads` threads numbered `t`.
+__device__ __forceinline__ void objective_part(const Hydro<double>& h, Field<double> u, double xc, double yc,
+                                               double sig, double* J, Field<double> ub, long long t,
+                                               long long nthreads) {
+  double acc = 0.0;
+  for (long long k = t; k < (long long)h.nx * h.ny; k += nthreads) {
+    const int i = GW + (int)(k % h.nx), j = GW + (int)(k / h.nx);
+    const double w = weight(h, i, j, xc, yc, sig);
+    const double r = u.at(ID, j, i);
+    acc += r * r * w;
+    if (ub.p) {
+      ub.at(ID, j, i) = 2.0 * r * w;
+      ub.at(IP, j, i) = 0.0;
+      ub.at(IU, j, i) = 0.0;
+      ub.at(IV, j, i) = 0.0;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(J, acc);
+}
+
+__global__ void k_objective(Hydro<double> h, Field<double> u, double xc, double yc, double sig, double* J,
+                            Field<double> ub) {
+  objective_part(h, u, xc, yc, sig, J, ub, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                 (long long)gridDim.x * blockDim.x);
+}
+
+// ---- batched kernels: every problem of an ensemble in one launch ----------
+
+__device__ __forceinline__ double* abuf(const AdjProb& P, int k) {
+  return k < 0 ? P.u0 : P.base + (long long)k * P.state_elems;
+}
+__device__ __forceinline__ Field<double> afield(const AdjProb& P, int k) {
+  return Field<double>{abuf(P, k), P.pitch, P.plane};
+}
+
+// Reverse step m of every problem: one CTA per 32 x 7 tile of the flattened
+// tile list (problem p owns tiles [tile_begin, tile_begin + ntx * nty)).
+__global__ void __launch_bounds__(ANT, 2)
+    k_batch_step_rev(const AdjProb* __restrict__ probs, int nprob, const double* dt_log, double* dtbar_log, int un,
+                     int ub_in, int ub_out, int m) {
+  extern __shared__ double sm[];
+  __shared__ Hydro<double> sh;
+  __shared__ int sp;
+  const int t = blockIdx.x;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nprob - 1;  // last problem with tile_begin <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].tile_begin <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    sp = lo;
+    sh = probs[lo].h;
+  }
+  __syncthreads();
+  const AdjProb& P = probs[sp];
+  const int tile = t - P.tile_begin;
+  const long long row = (long long)m * nprob + sp;
+  step_rev_tile(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out), dt_log[row], dtbar_log + row,
+                tile % P.ntx, tile / P.ntx, sm);
+}
+
+__global__ void k_batch_argmax(const AdjProb* __restrict__ probs, int nprob, const double* inv_log, int un, int m,
+                               double* pv, long long* pi) {
+  const int p = blockIdx.y;
+  if (!max_rises(inv_log + p, m, nprob)) return;
+  const AdjProb& P = probs[p];
+  argmax_part(P.h, afield(P, un), blockIdx.x, gridDim.x, pv + (long long)p * gridDim.x,
+              pi + (long long)p * gridDim.x);
+}
+
+__global__ void k_batch_dt_route(const AdjProb* __restrict__ probs, int nprob, const double* pv, const long long* pi,
+                                 int nparts, const double* dtbar_log, const double* inv_log, int un, int ub_out,
+                                 int m, int nsteps) {
+  const int p = blockIdx.x;
+  if (threadIdx.x != 0 || !max_rises(inv_log + p, m, nprob)) return;
+  const AdjProb& P = probs[p];
+  dt_route(P.h, afield(P, un), afield(P, ub_out), pv + (long long)p * nparts, pi + (long long)p * nparts, nparts,
+           dtbar_log + p, inv_log + p, nprob, m, nsteps);
+}
+
+__global__ void k_batch_objective(const AdjProb* __restrict__ probs, int un, double xc, double yc, double sig,
+                                  double* J, int seed_ub) {
+  const int p = blockIdx.y;
+  const AdjProb& P = probs[p];
+  Field<double> ub = seed_ub >= 0 ? afield(P, seed_ub) : Field<double>{nullptr, 0, 0};
+  objective_part(P.h, afield(P, un), xc, yc, sig, J + p, ub, blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                 (long long)gridDim.x * blockDim.x);
+}
+
+// Whole-buffer copy (src < 0: the initial state) or zero fill (src == dst);
+// state_elems is a multiple of 32, so double2 accesses stay aligned.
+__global__ void k_batch_copy(const AdjProb* __restrict__ probs, int src, int dst) {
+  const AdjProb& P = probs[blockIdx.y];
+  double2* d = reinterpret_cast<double2*>(abuf(P, dst));
+  const double2* sp = reinterpret_cast<const double2*>(abuf(P, src));
+  const long long n = P.state_elems / 2;
+  const bool zero = src == dst;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    d[k] = zero ? make_double2(0.0, 0.0) : sp[k];
+}
+
+__global__ void k_batch_seg_corners(const AdjProb* __restrict__ probs, int ping, int seg, int k0) {
+  const AdjProb& P = probs[blockIdx.y];
+  const int j = blockIdx.x + 1;
+  if (threadIdx.x >= 64) return;
+  copy_corner(abuf(P, ping + ((k0 + j) & 1)), abuf(P, seg + j), P.pitch, P.plane, P.h.isize, P.h.jsize,
+              threadIdx.x);
+}
+
+// Interior density adjoints of buffer ub into the packed output (i fastest).
+__global__ void k_batch_extract(const AdjProb* __restrict__ probs, int ub, double* out) {
+  const AdjProb& P = probs[blockIdx.y];
+  const double* src = abuf(P, ub);
+  const long long n = (long long)P.h.nx * P.h.ny;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = GW + (int)(k % P.h.nx), j = GW + (int)(k / P.h.nx);
+    out[P.grad_off + k] = src[(long long)j * P.pitch + i];
+  }
+}
+
+}  // namespace
+
+size_t step_rev_smem() { return SMEM_BYTES; }
+
+int step_rev_setup() {
+  return cudaFuncSetAttribute(k_step_rev, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
+                 cudaSuccess
+             ? 0
+             : -1;
+}
+
+void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn1, Field<double> ubn,
+                     const double* dt, double* dtbar, cudaStream_t s) {
+  dim3 g((h.nx + ATX - 1) / ATX, (h.ny + ATY - 1) / ATY);
+  k_step_rev<<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, dt, dtbar);
+}
+
+void launch_seg_corners(const Hydro<double>& h, double* pool, size_t state_elems, size_t pitch, size_t plane,
+                        int ping_index, int seg_index, int k0, int nseg, cudaStream_t s) {
+  if (nseg > 1)
+    k_seg_corners<<<nseg - 1, 64, 0, s>>>(pool, (long long)state_elems, (int)pitch, (long long)plane, h.isize,
+                                          h.jsize, ping_index, seg_index, k0);
+}
+
+void launch_argmax(const Hydro<double>& h, Field<double> u, double* pv, long long* pi, int nparts,
+                   const double* inv_log, int m, cudaStream_t s) {
+  k_argmax_partial<<<nparts, 256, 0, s>>>(h, u, pv, pi, inv_log, m);
+}
+
+void launch_dt_route(const Hydro<double>& h, Field<double> u, Field<double> ub, const double* pv, const long long* pi,
+                     int nparts, const double* dtbar_log, const double* inv_log, int m, int nsteps,
+                     cudaStream_t s) {
+  k_dt_route<<<1, 32, 0, s>>>(h, u, ub, pv, pi, nparts, dtbar_log, inv_log, m, nsteps);
+}
+
+void launch_objective(const Hydro<double>& h, Field<double> u, double xc, double yc, double sig, double* J,
+                      Field<double> ub, cudaStream_t s) {
+  k_objective<<<256, 256, 0, s>>>(h, u, xc, yc, sig, J, ub);
+}
+
+int batch_step_rev_setup() {
+  return cudaFuncSetAttribute(k_batch_step_rev, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
+                 cudaSuccess
+             ? 0
+             : -1;
+}
+
+int rev_tile_shape(int* tx, int* ty) {
+  *tx = ATX;
+  *ty = ATY;
+  return 0;
+}
+
+void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int m, cudaStream_t s) {
+  k_batch_step_rev<<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in, ub_out,
+                                                          m);
+}
+
+void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s) {
+  k_batch_argmax<<<dim3(B.nparts, B.nprob), 256, 0, s>>>(B.probs, B.nprob, B.inv_log, un, m, B.part_v, B.part_i);
+}
+
+void launch_batch_dt_route(const AdjBatch& B, int un, int ub_out, int m, int nsteps, cudaStream_t s) {
+  k_batch_dt_route<<<B.nprob, 32, 0, s>>>(B.probs, B.nprob, B.part_v, B.part_i, B.nparts, B.dtbar_log, B.inv_log, un,
+                                          ub_out, m, nsteps);
+}
+
+void launch_batch_objective(const AdjBatch& B, int un, double xc, double yc, double sig, int seed_ub,
+                            cudaStream_t s) {
+  k_batch_objective<<<dim3(64, B.nprob), 256, 0, s>>>(B.probs, un, xc, yc, sig, B.J, seed_ub);
+}
+
+void launch_batch_copy(const AdjBatch& B, int src, int dst, cudaStream_t s) {
+  k_batch_copy<<<dim3(64, B.nprob), 256, 0, s>>>(B.probs, src, dst);
+}
+
+void launch_batch_seg_corners(const AdjBatch& B, int ping, int seg, int k0, int nseg, cudaStream_t s) {
+  if (nseg > 1) k_batch_seg_corners<<<dim3(nseg - 1, B.nprob), 64, 0, s>>>(B.probs, ping, seg, k0);
+}
+
+void launch_batch_extract(const AdjBatch& B, int ub, double* out, cudaStream_t s) {
+  k_batch_extract<<<dim3(32, B.nprob), 256, 0, s>>>(B.probs, ub, out);
+}
+
+}  // namespace e2d

@@ -1,0 +1,135 @@
+// k_batch.cu -- one kernel launch advances a whole ensemble of independent
+// problems of uneven sizes by one time step.
+//
+// The tiles of every problem form one flattened work list (problem p owns
+// tiles [tile_begin[p], tile_begin[p+1])); a persistent grid of CTAs walks
+// the list with a fixed stride.  Each tile is computed exactly as in the
+// single-run kernel (tile.cuh) with its own problem's parameters, its own dt
+// (from the problem's running CFL maximum) and its own ghost rules, and
+// folds the next step's CFL maximum into the problem's own slot.  The box is
+// loaded with coalesced plain loads because every problem has its own array.
+#include "batch.h"
+#include "tile.cuh"
+
+namespace e2d {
+
+namespace {
+
+template <typename Real, class C, int MINB>
+__global__ void __launch_bounds__(C::NT, MINB)
+    k_batch_step(const BatchProb<Real>* __restrict__ probs, int nprob, int total_tiles, int parity, int rd, int wr,
+                 Ctl* ctls, Real* dt_log, const Real* dt_src, Real* inv_log) {
+  extern __shared__ unsigned char smem_raw[];
+  Real* base = reinterpret_cast<Real*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  unsigned char* tail = reinterpret_cast<unsigned char*>(base + C::n_real);
+  int* face_counter = reinterpret_cast<int*>(tail + 8);
+  Real* red = reinterpret_cast<Real*>(tail + 16);
+  Real* sdt = red + 32;
+  __shared__ Hydro<Real> sh;
+  __shared__ int sp, sid, stile;
+  const int tid = threadIdx.x;
+
+  for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+    if (tid == 0) {
+      int lo = 0, hi = nprob - 1;  // last problem with tile_begin <= t
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (probs[mid].tile_begin <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      sp = lo;
+      sid = probs[lo].id;
+      stile = t - probs[lo].tile_begin;
+      sh = probs[lo].h;
+      *face_counter = 0;
+      const Real dt0 = dt_src ? dt_src[sid] : sh.cfl / *inv_slot<Real>(&ctls[sid], rd);
+      sdt[0] = dt0;
+      sdt[1] = dt0 / sh.dx;
+      sdt[2] = dt0 / sh.dy;
+    }
+    __syncthreads();
+    const int p = sp, id = sid;
+    const BatchProb<Real>& P = probs[p];
+    const int tx = stile % P.ntx, ty = stile / P.ntx;
+    const int i0 = GW + tx * C::TX, j0 = GW + ty * C::TY;
+    Field<Real> in{parity ? P.u2 : P.u, P.pitch, P.plane};
+    Field<Real> out{parity ? P.u : P.u2, P.pitch, P.plane};
+    // conservative box, zero outside the array (what TMA zero fill gives)
+    Real* sq = base + C::q_off;
+    for (int k = tid; k < 4 * C::BYs * C::BXs; k += C::NT) {
+      const int v = k / (C::BYs * C::BXs), rem = k - v * (C::BYs * C::BXs);
+      const int y = rem / C::BXs, x = rem - y * C::BXs;
+      const int gi = i0 - GW + x, gj = j0 - GW + y;
+      sq[k] = (gi < sh.isize && gj < sh.jsize) ? in.at(v, gj, gi) : Real(0);
+    }
+    __syncthreads();
+    Real m = tile_compute<Real, C>(sh, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2], true, wr >= 0,
+                                   &ctls[id].health);
+    if (tid == 0) {
+      if (stile == 0) {
+        if (dt_log) dt_log[id] = sdt[0];
+        if (inv_log) inv_log[id] = *inv_slot<Real>(&ctls[id], rd);
+        if (!isfinite(sdt[0])) atomicOr(&ctls[id].health, 1u);
+      }
+      if (wr >= 0) {
+        m = fmax(m, *inv_slot<Real>(&ctls[id], rd));
+        atomic_max_slot_ptr<Real>(inv_slot<Real>(&ctls[id], wr), m);
+      }
+    }
+    __syncthreads();  // shared memory is reused by the next tile
+  }
+}
+
+template <typename Real, class C, int MINB>
+struct Variant {
+  static int resident_per_sm() {
+    int n = 0;
+    if (cudaFuncSetAttribute(k_batch_step<Real, C, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)C::bytes) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<Real, C, MINB>, C::NT, C::bytes) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    return n;
+  }
+  static void launch(const BatchLaunch<Real>& L, cudaStream_t s) {
+    k_batch_step<Real, C, MINB><<<L.grid, C::NT, C::bytes, s>>>(L.probs, L.nprob, L.total_tiles, L.parity, L.rd,
+                                                                L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+  }
+};
+
+// Tile shapes offered to the autotuner.
+template <typename Real> using V32x15 = Variant<Real, TileCfg<Real, 32, 15, 256>, (sizeof(Real) == 8 ? 2 : 3)>;
+template <typename Real> using V32x7 = Variant<Real, TileCfg<Real, 32, 7, 128>, (sizeof(Real) == 8 ? 4 : 6)>;
+
+}  // namespace
+
+template <typename Real>
+int batch_tile_shape(int variant, int* tx, int* ty, int* nt) {
+  switch (variant) {
+    case 0: *tx = 32; *ty = 15; *nt = 256; return 0;
+    case 1: *tx = 32; *ty = 7; *nt = 128; return 0;
+    default: return -1;
+  }
+}
+
+template <typename Real>
+int batch_resident_per_sm(int variant) {
+  return variant == 0 ? V32x15<Real>::resident_per_sm() : V32x7<Real>::resident_per_sm();
+}
+
+template <typename Real>
+void launch_batch_step(int variant, const BatchLaunch<Real>& L, cudaStream_t s) {
+  if (variant == 0) V32x15<Real>::launch(L, s);
+  else V32x7<Real>::launch(L, s);
+}
+
+template int batch_tile_shape<double>(int, int*, int*, int*);
+template int batch_tile_shape<float>(int, int*, int*, int*);
+template int batch_resident_per_sm<double>(int);
+template int batch_resident_per_sm<float>(int);
+template void launch_batch_step<double>(int, const BatchLaunch<double>&, cudaStream_t);
+template void launch_batch_step<float>(int, const BatchLaunch<float>&, cudaStream_t);
+
+}  // namespace e2d

@@ -16,6 +16,7 @@ inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) /
 
 template <typename Real>
 __device__ __forceinline__ Real resolve_dt(const Hydro<Real>& h, const StepDt<Real>& sd, Ctl* ctl) {
+  if (sd.dt_ptr) return *sd.dt_ptr;
   if (sd.from_slot) return Ops<Real>::div(h.cfl, *inv_slot<Real>(ctl, sd.rd_slot));
   return sd.dt_value;
 }

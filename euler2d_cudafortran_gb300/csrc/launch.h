@@ -28,6 +28,7 @@ template <> __host__ __device__ inline float* inv_slot<float>(Ctl* c, int s) { r
 template <typename Real>
 struct StepDt {
   Real dt_value;
+  const Real* dt_ptr;  // when set, dt is read from this device address (a logged dt)
   int from_slot;    // 1: dt = cfl / inv[rd_slot]
   int rd_slot;      // slot holding the running max for this step's dt
   int wr_slot;      // slot receiving max(inv[rd], max over the new state); -1: no reduction
@@ -67,5 +68,11 @@ void fused_plan_destroy(FusedPlan* p);
 template <typename Real> void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in,
                                            Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
                                            cudaStream_t s);
+// A TMA descriptor for any pitched state (used for states outside a run's u/u2).
+struct StateMap { alignas(64) unsigned char bytes[128]; };
+template <typename Real> bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out);
+template <typename Real> void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in,
+                                               Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
+                                               cudaStream_t s);
 
 }  // namespace e2d

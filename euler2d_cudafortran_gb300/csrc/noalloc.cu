@@ -82,6 +82,7 @@ int step(const e2d_params& p, void* u_in, void* u_out, size_t pitch, double dt, 
   Field<Real> fy{base + 8 * wplane, (int)work_pitch, wplane};
   StepDt<Real> sd;
   sd.dt_value = (Real)dt;
+  sd.dt_ptr = nullptr;
   sd.from_slot = 0;
   sd.rd_slot = -1;
   sd.wr_slot = -1;

@@ -1,0 +1,209 @@
+// tile.cuh -- the fused Godunov step of one tile, shared by the single-run
+// kernel (k_fused.cu, TMA-loaded tiles) and the batched kernel (k_batch.cu).
+//
+// A CTA owns a TX x TY tile of interior cells whose conservative box
+// [i0-2, i0+TX+2) x [j0-2, j0+TY+2) x 4 already sits in shared memory
+// (outside the domain it holds zeros, as TMA zero fill gives).  tile_compute
+//   - converts the box to primitives in place (computePrimitives),
+//   - computes slopes (slope_unsplit_hydro_2d) and trace source terms once
+//     per cell of the (TX+2) x (TY+2) ring,
+//   - solves the (TX+1) x TY x-faces and TX x (TY+1) y-faces (face states of
+//     trace_unsplit_2d_along_dir, the Riemann flux, times dt/dx or dt/dy),
+//     warps claiming 32 faces at a time,
+//   - applies updateHydro, writes the tile of the new state, the ghost cells
+//     make_boundaries would copy from it (when asked), raises the health
+//     flags, and returns the block maximum of the next step's CFL term.
+#pragma once
+#include "launch.h"
+
+namespace e2d {
+
+template <typename Real, int TX_, int TY_, int NT_>
+struct TileCfg {
+  static constexpr int TX = TX_, TY = TY_, NT = NT_;
+  static constexpr int BXs = TX + 4, BYs = TY + 4;  // conservative box
+  static constexpr int RX = TX + 2, RY = TY + 2;    // ring of cells with slopes
+  static constexpr size_t q_off = 0;                              // [4][BYs][BXs]
+  static constexpr size_t d_off = q_off + 4ull * BYs * BXs;       // [8][RY][RX]
+  static constexpr size_t s_off = d_off + 8ull * RY * RX;         // [4][RY][RX]
+  static constexpr size_t fx_off = s_off + 4ull * RY * RX;        // [4][TY][TX+1]
+  static constexpr size_t fy_off = fx_off + 4ull * TY * (TX + 1); // [4][TY+1][TX]
+  static constexpr size_t n_real = fy_off + 4ull * (TY + 1) * TX;
+  // after the reals: mbarrier (8 B), face counter (8 B), warp maxima (32 reals), dt values (4 reals)
+  static constexpr size_t bytes = n_real * sizeof(Real) + 16 + 36 * sizeof(Real) + 128;
+  static constexpr uint32_t box_bytes = 4u * BYs * BXs * sizeof(Real);
+  static_assert((n_real * sizeof(Real)) % 8 == 0, "mbarrier alignment");
+};
+
+// Source cell of ghost column/row g along one axis of n interior cells for
+// boundary type `type` (serial_ref/m_run.f90:573-644), 0-based; g in
+// {0, 1, n+2, n+3}.
+__device__ __forceinline__ int ghost_source(int g, int n, int type) {
+  if (g < 2) return (type == 1) ? 3 - g : (type == 2) ? 2 : n + g;
+  return (type == 1) ? 2 * n + 3 - g : (type == 2) ? n + 1 : g - n;
+}
+
+template <typename Real>
+__device__ __forceinline__ void atomic_max_slot_ptr(Real* slot, Real m);
+template <>
+__device__ __forceinline__ void atomic_max_slot_ptr<double>(double* slot, double m) {
+  atomicMax(reinterpret_cast<unsigned long long*>(slot), ordered_bits(m));
+}
+template <>
+__device__ __forceinline__ void atomic_max_slot_ptr<float>(float* slot, float m) {
+  atomicMax(reinterpret_cast<unsigned int*>(slot), ordered_bits(m));
+}
+
+// Phases 2-5 for the tile at (i0, j0); all threads call it after the box is
+// in base[q_off..].  *face_counter must be 0.  Returns, in thread 0, the
+// block maximum of the CFL term of the new state (0 when !want_dt).
+template <typename Real, class C>
+__device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
+                                             int i0, int j0, const Field<Real>& in, const Field<Real>& out,
+                                             Real dtdx, Real dtdy, bool fill_ghosts, bool want_dt,
+                                             unsigned* health) {
+  constexpr int TX = C::TX, TY = C::TY, NT = C::NT, BXs = C::BXs, BYs = C::BYs, RX = C::RX, RY = C::RY;
+  Real* sq = base + C::q_off;
+  Real* sdq = base + C::d_off;
+  Real* ss = base + C::s_off;
+  Real* sfx = base + C::fx_off;
+  Real* sfy = base + C::fy_off;
+  const int tid = threadIdx.x;
+
+  // ---- primitives of the whole box, in place (computePrimitives)
+  for (int k = tid; k < BXs * BYs; k += NT) {
+    Real u[4], q[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) u[v] = sq[v * BXs * BYs + k];
+    primitives(h, u, q);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sq[v * BXs * BYs + k] = q[v];
+  }
+  __syncthreads();
+
+  // ---- slopes and trace source terms of the ring cells (-1..TX, -1..TY)
+  auto Q = [&](int v, int y, int x) -> Real { return sq[(v * BYs + y) * BXs + x]; };
+  for (int k = tid; k < RX * RY; k += NT) {
+    const int x = k % RX + 1, y = k / RX + 1;  // box coordinates
+    Real qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qc[v] = Q(v, y, x); qe[v] = Q(v, y, x + 1); qw[v] = Q(v, y, x - 1);
+      qn[v] = Q(v, y + 1, x); qs[v] = Q(v, y - 1, x);
+    }
+    slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
+    trace_sources(h, qc, dqx, dqy, s);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      sdq[v * RX * RY + k] = dqx[v];
+      sdq[(4 + v) * RX * RY + k] = dqy[v];
+      ss[v * RX * RY + k] = s[v];
+    }
+  }
+  __syncthreads();
+
+  // ---- Riemann fluxes of all faces of the tile, claimed 32 at a time per warp
+  constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1), NF = NXF + NYF;
+  const int lane = tid & 31;
+  while (true) {
+    int chunk = 0;
+    if (lane == 0) chunk = atomicAdd(face_counter, 32);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk >= NF) break;
+    const int k = chunk + lane;
+    if (k < NXF) {
+      const int f = k % (TX + 1), r = k / (TX + 1);  // between ring cells (f-1, r) and (f, r)
+      if (i0 + f <= h.nx + 2 && j0 + r <= h.ny + 1) {
+        const int kl = (r + 1) * RX + f, kr = kl + 1;
+        Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 1); dq[v] = sdq[v * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
+        trace_face<Real, true>(h, qc, dq, s, dtdx, ql);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 2); dq[v] = sdq[v * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
+        trace_face<Real, false>(h, qc, dq, s, dtdx, qr);
+        riemann(h, ql, qr, flux);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = mul<MS_FLUX>(flux[v], dtdx);
+      }
+    } else if (k < NF) {
+      const int kk = k - NXF;
+      const int c = kk % TX, g = kk / TX;  // between ring cells (c, g-1) and (c, g)
+      if (i0 + c <= h.nx + 1 && j0 + g <= h.ny + 2) {
+        const int kl = g * RX + (c + 1), kr = kl + RX;
+        Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 1, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
+        trace_face<Real, true>(h, qc, dq, s, dtdy, ql);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 2, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
+        trace_face<Real, false>(h, qc, dq, s, dtdy, qr);
+        Real t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
+        t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
+        riemann(h, ql, qr, flux);
+        t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sfy[(v * (TY + 1) + g) * TX + c] = mul<MS_FLUX>(flux[v], dtdy);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- updateHydro + ghost copies + next-step CFL maximum
+  Real m = Real(0);
+  for (int k = tid; k < TX * TY; k += NT) {
+    const int c = k % TX, r = k / TX;
+    const int i = i0 + c, j = j0 + r;
+    if (i > h.nx + 1 || j > h.ny + 1) continue;
+    Real un[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      Real flux_tot = sfx[(v * TY + r) * (TX + 1) + c] - sfx[(v * TY + r) * (TX + 1) + c + 1];
+      flux_tot = (sfy[(v * (TY + 1) + r) * TX + c] - sfy[(v * (TY + 1) + r + 1) * TX + c]) + flux_tot;
+      un[v] = in.at(v, j, i) + flux_tot;
+      out.at(v, j, i) = un[v];
+    }
+    if (fill_ghosts) {
+      if (i <= 3 || i >= h.nx) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int g = (e < 2) ? e : h.nx + e;
+          const int type = (e < 2) ? h.bc_xmin : h.bc_xmax;
+          if (ghost_source(g, h.nx, type) == i) {
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+              out.at(v, j, g) = un[v] * ((type == 1 && v == IU) ? Real(-1.0) : Real(1.0));
+          }
+        }
+      }
+      if (j <= 3 || j >= h.ny) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int g = (e < 2) ? e : h.ny + e;
+          const int type = (e < 2) ? h.bc_ymin : h.bc_ymax;
+          if (ghost_source(g, h.ny, type) == j) {
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+              out.at(v, g, i) = un[v] * ((type == 1 && v == IV) ? Real(-1.0) : Real(1.0));
+          }
+        }
+      }
+    }
+    if (!(un[ID] > Real(0)) || !isfinite(un[ID])) atomicOr(health, 2u);
+    if (want_dt && i <= h.isize - 4 && j <= h.jsize - 4) m = Ops<Real>::max(m, cell_invdt(h, un));
+  }
+  if (want_dt) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) red[tid >> 5] = m;
+    __syncthreads();
+    if (tid < 32) {
+      m = (tid < NT / 32) ? red[tid] : Real(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+  }
+  return m;
+}
+
+}  // namespace e2d

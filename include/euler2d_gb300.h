@@ -134,10 +134,12 @@ int e2d_time_steps(e2d_run* h, int nStep0, int nsteps, float* ms);
  * the FP64 step.  Not part of the reference; used by the benchmark. */
 int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
 
-/* Self-test of the library's integer-pipe double division (op 0) and square
- * root (op 1) against the hardware operations on n seeded inputs (mode 0 any
- * bit pattern, 1 exponents near 1, 2 exponents within +-400, 3 results next to
- * rounding boundaries, 4 signed zeros and small integers): *mismatches counts results that differ in any bit,
+/* Self-test of the library's integer-pipe double division (op 0), square
+ * root (op 1) and multiplication (op 2) against the hardware operations on n
+ * seeded inputs (mode 0 any bit pattern, 1 exponents near 1, 2 exponents
+ * within +-400, 3 results next to rounding boundaries or, for the
+ * multiplication, exact products and ties, 4 signed zeros and small
+ * integers): *mismatches counts results that differ in any bit,
  * first_bad[4] (optional) = a, b, emulated, hardware of the first one; the
  * two rates (optional) are chained operations per second.  Not part of the
  * reference; used by the tests. */
@@ -157,6 +159,85 @@ const char* e2d_last_error(void);
  * keep the state resident, with the row pitch in elements and plane stride. */
 int e2d_device_state(e2d_run* h, int which, void** dptr, size_t* pitch_elems,
                      size_t* plane_elems);
+
+/* ---- Batched ensemble: many independent runs of uneven sizes ----
+ * No counterpart in the reference (which runs one problem per process): the
+ * step of each problem is the one of e2d_godunov_unsplit with
+ * implementationVersion 0 arithmetic, each problem has its own dt, running
+ * CFL maximum, boundary types and ping-pong pair, and one kernel launch
+ * advances every problem by one step (the tiles of all problems form one
+ * work list walked by a persistent grid).  Problem p's states are selected by
+ * `prob`; layouts as for single runs. */
+typedef struct e2d_batch e2d_batch;
+
+/* nprob problems with sizes nx[p] x ny[p]; bc (optional) holds 4 boundary
+ * types per problem (xmin, xmax, ymin, ymax); the other fields come from base. */
+int e2d_batch_create(const e2d_params* base, int nprob, const int* nx, const int* ny, const int* bc,
+                     e2d_batch** out);
+int e2d_batch_destroy(e2d_batch* b);
+/* Diagonal interface per problem (e2d_init_diagonal with per-problem arrays). */
+int e2d_batch_init_diagonal(e2d_batch* b, const double* offset, const double* rho_hi, const double* p_hi,
+                            const double* rho_lo, const double* p_lo);
+int e2d_batch_upload_state(e2d_batch* b, int prob, int which, const void* host);
+int e2d_batch_download_state(e2d_batch* b, int prob, int which, void* host);
+/* e2d_advance for every problem at once; dt_log (optional) receives
+ * nsteps x nprob values (step-major). */
+int e2d_batch_advance(e2d_batch* b, int nStep0, int nsteps, void* dt_log);
+int e2d_batch_last_advance_ms(e2d_batch* b, float* ms);
+/* Schedule: variant 0 = 32x15-cell tiles, 1 = 32x7; grid_mult x resident CTAs
+ * per SM x SMs persistent CTAs; order 0 = problem order, 1 = largest first. */
+int e2d_batch_set_schedule(e2d_batch* b, int variant, int grid_mult, int order);
+int e2d_batch_get_schedule(e2d_batch* b, int* variant, int* grid_mult, int* order, int* grid);
+/* Autotuner: times every schedule on `steps` steps of the current states
+ * (restored afterwards) and keeps the fastest; with cache_path, reuses and
+ * records choices per ensemble shape. */
+int e2d_batch_tune(e2d_batch* b, int steps, const char* cache_path, float* best_ms);
+int e2d_batch_get_health(e2d_batch* b, int prob, unsigned* flags);
+
+/* ---- Discrete adjoint (FP64, HLLC flux) ----
+ * No counterpart in the reference.  Gradient of J = sum over interior cells of
+ * rho^2 w(x, y) after nsteps steps, w(x, y) = exp(-((x-xc)^2 + (y-yc)^2) /
+ * (2 sigma^2)) at cell centres x = (i + 1/2) dx, with respect to the initial
+ * density of the interior cells, by hand-written reverse kernels of every
+ * stage of the step and ceil(sqrt(nsteps)) state checkpoints with
+ * recomputation.  dt_mode 0 keeps the dt of every step frozen; 1 also
+ * differentiates dt = cfl / (running CFL maximum).  u0 is the initial state
+ * (Fortran layout, ghosts included) or NULL for init_implode. */
+typedef struct e2d_adjoint e2d_adjoint;
+int e2d_adjoint_create(const e2d_params* p, e2d_adjoint** out);
+int e2d_adjoint_destroy(e2d_adjoint* a);
+/* J only (the forward run), e.g. for finite differences; with dt_fixed
+ * (nsteps values) step n uses dt_fixed[n] instead of the CFL dt. */
+int e2d_adjoint_objective(e2d_adjoint* a, const void* u0, int nsteps, double xc, double yc, double sigma,
+                          const double* dt_fixed, double* J);
+/* J and dJ/d rho0 (nx*ny values, i fastest); dt_log (optional) gets the dt of each step. */
+int e2d_adjoint_gradient(e2d_adjoint* a, const void* u0, int nsteps, int dt_mode, double xc, double yc,
+                         double sigma, double* J, double* grad_rho0, double* dt_log);
+/* Device times (ms) of the last objective and gradient calls. */
+int e2d_adjoint_last_ms(e2d_adjoint* a, float* objective_ms, float* gradient_ms);
+
+/* ---- Batched adjoint: the adjoint of many independent problems at once ----
+ * No counterpart in the reference.  Problems of uneven sizes (FP64, HLLC),
+ * each with its own initial state, boundaries, dt and running CFL maximum,
+ * all advanced by the same number of steps; each stage of the forward and
+ * reverse sweeps is one launch over every problem, and one call is one
+ * captured CUDA graph.  J_p and dJ_p/d rho0_p are as for e2d_adjoint_gradient;
+ * the gradients are packed problem after problem (nx[p]*ny[p] values each,
+ * i fastest), dt_log (optional) gets nsteps x nprob values (step-major). */
+typedef struct e2d_adjoint_batch e2d_adjoint_batch;
+int e2d_adjoint_batch_create(const e2d_params* base, int nprob, const int* nx, const int* ny, const int* bc,
+                             e2d_adjoint_batch** out);
+int e2d_adjoint_batch_destroy(e2d_adjoint_batch* b);
+/* Initial states: diagonal interfaces with per-problem data, or one problem's
+ * full state (Fortran layout, ghosts included). */
+int e2d_adjoint_batch_init_diagonal(e2d_adjoint_batch* b, const double* offset, const double* rho_hi,
+                                    const double* p_hi, const double* rho_lo, const double* p_lo);
+int e2d_adjoint_batch_upload_state(e2d_adjoint_batch* b, int prob, const void* host);
+/* The forward runs only (no checkpoints): J[nprob]. */
+int e2d_adjoint_batch_objective(e2d_adjoint_batch* b, int nsteps, double xc, double yc, double sigma, double* J);
+int e2d_adjoint_batch_gradient(e2d_adjoint_batch* b, int nsteps, int dt_mode, double xc, double yc, double sigma,
+                               double* J, double* grad_rho0, double* dt_log);
+int e2d_adjoint_batch_last_ms(e2d_adjoint_batch* b, float* objective_ms, float* gradient_ms);
 
 /* One godunov_unsplit step (the stored-fluxes variant, implementationVersion 2
  * arithmetic) that allocates no device memory.  No counterpart in the

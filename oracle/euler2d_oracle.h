@@ -75,6 +75,15 @@ int oracle_run_f64(const oracle_params* p, int nsteps, double* u, double* u2,
 int oracle_run_f32(const oracle_params* p, int nsteps, float* u, float* u2,
                    float* invdt, float* dt_log, int nthreads);
 
+/* J = sum over interior cells of rho^2 w(x, y) (Gaussian w of width sig at (xc, yc)). */
+double oracle_objective_f64(const oracle_params* p, const double* u, double xc, double yc, double sig);
+
+/* euler2d_oracle.c also exports a complex-step (forward-mode tangent) build of
+ * the same routines with the suffix _c128 (oracle_run_c128,
+ * oracle_objective_c128, ...): arguments as for _f64 with every double array
+ * or scalar of the state replaced by double complex; the imaginary parts
+ * carry the directional derivatives. */
+
 /* ---- pointwise routines (serial_ref/m_utils.f90), for unit tests ---- */
 void oracle_primitives_f64(const oracle_params* p, const double u[4], double q[4], double* c);
 void oracle_primitives_f32(const oracle_params* p, const float u[4], float q[4], float* c);

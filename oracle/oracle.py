@@ -154,6 +154,58 @@ def run(p: Params, nsteps: int, prec: str = "f64", u0: np.ndarray | None = None,
     return final, dt_log[:nsteps], u, u2
 
 
+# ---- objective and its forward-mode tangent ----------------------------------
+
+def objective(p: Params, u: np.ndarray, xc=0.6, yc=0.6, sig=0.1) -> float:
+    """J = sum over interior cells of rho^2 w, w a Gaussian at cell centres."""
+    f = lib().oracle_objective_f64
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    return f(ctypes.byref(p.c()), _ptr(np.ascontiguousarray(u, dtype=np.float64)), xc, yc, sig)
+
+
+def run_fixed_dt(p: Params, u0: np.ndarray, dts, nthreads: int = 1):
+    """The driver loop with the dt of every step given (dt frozen); final state."""
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    u2 = new_state(p)
+    d = np.ascontiguousarray(dts, dtype=np.float64)
+    rc = lib().oracle_run_fixed_dt_f64(ctypes.byref(p.c()), ctypes.c_int(len(d)), _ptr(u), _ptr(u2), _ptr(d),
+                                      ctypes.c_int(nthreads))
+    if rc != 0:
+        raise MemoryError("oracle_run_fixed_dt failed")
+    return u if len(d) % 2 == 0 else u2
+
+
+def tangent(p: Params, u0: np.ndarray, direction: np.ndarray, nsteps: int, xc=0.6, yc=0.6, sig=0.1,
+            h: float = 1e-200, nthreads: int = 1, fixed_dts=None):
+    """Forward-mode derivative of J(final state) along a perturbation of the
+    initial interior density: the complex-step build of the oracle run from
+    u0 + i h d (d on the density plane's interior).  With fixed_dts the dt
+    of every step is frozen.  Returns (J, dJ.d)."""
+    uc = np.ascontiguousarray(u0, dtype=np.complex128).copy()
+    uc[0, 2:-2, 2:-2] += 1j * h * direction
+    u2 = np.zeros_like(uc)
+    inv = np.zeros(1, dtype=np.complex128)
+    dts = np.zeros(max(nsteps, 1), dtype=np.complex128)
+    L = lib()
+    if fixed_dts is not None:
+        fd = np.ascontiguousarray(fixed_dts[:nsteps], dtype=np.float64)
+        rc = L.oracle_run_fixed_dt_c128(ctypes.byref(p.c()), ctypes.c_int(nsteps), _ptr(uc), _ptr(u2), _ptr(fd),
+                                        ctypes.c_int(nthreads))
+    else:
+        rc = L.oracle_run_c128(ctypes.byref(p.c()), ctypes.c_int(nsteps), _ptr(uc), _ptr(u2), _ptr(inv),
+                               _ptr(dts), ctypes.c_int(nthreads))
+    if rc != 0:
+        raise MemoryError("oracle_run_c128 failed")
+    final = uc if nsteps % 2 == 0 else u2
+    out = np.zeros(1, dtype=np.complex128)
+    f = L.oracle_objective_into_c128
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_void_p]
+    f(ctypes.byref(p.c()), _ptr(final), xc, yc, sig, _ptr(out))
+    return out[0].real, out[0].imag / h
+
+
 # ---- pointwise routines ----------------------------------------------------
 
 def _vec(x, prec):

@@ -84,3 +84,33 @@ def test_create_without_device_fails_cleanly(e2d):
     p.nx = p.ny = 16
     h = ctypes.c_void_p()
     assert e2d.load_library().e2d_create(ctypes.byref(p), ctypes.byref(h)) == e2d.E2D_ERR_NO_DEVICE
+
+
+def test_batch_create_rejects_invalid_arguments(e2d):
+    lib = e2d.load_library()
+    p = e2d.default_params()
+    h = ctypes.c_void_p()
+    nx = (ctypes.c_int * 2)(16, 1)
+    ny = (ctypes.c_int * 2)(16, 16)
+    assert lib.e2d_batch_create(ctypes.byref(p), 2, nx, ny, None, ctypes.byref(h)) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_batch_create(ctypes.byref(p), 0, nx, ny, None, ctypes.byref(h)) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_batch_destroy(None) == e2d.E2D_OK
+    assert lib.e2d_batch_advance(None, 0, 1, None) == e2d.E2D_ERR_INVALID_ARG
+
+
+def test_adjoint_create_rejects_invalid_arguments(e2d):
+    lib = e2d.load_library()
+    h = ctypes.c_void_p()
+    p = e2d.make_params(nx=16, ny=16, riemann_solver=e2d.RIEMANN_APPROX)
+    assert lib.e2d_adjoint_create(ctypes.byref(p), ctypes.byref(h)) == e2d.E2D_ERR_INVALID_ARG  # HLLC only
+    p = e2d.make_params(nx=16, ny=16, riemann_solver=e2d.RIEMANN_HLLC, precision=4)
+    assert lib.e2d_adjoint_create(ctypes.byref(p), ctypes.byref(h)) == e2d.E2D_ERR_INVALID_ARG  # FP64 only
+    p = e2d.make_params(nx=16, ny=16, riemann_solver=e2d.RIEMANN_HLLC)
+    nx = (ctypes.c_int * 2)(16, 1)
+    ny = (ctypes.c_int * 2)(16, 16)
+    assert lib.e2d_adjoint_batch_create(ctypes.byref(p), 2, nx, ny, None, ctypes.byref(h)) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_adjoint_batch_create(ctypes.byref(p), 0, nx, ny, None, ctypes.byref(h)) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_adjoint_destroy(None) == e2d.E2D_OK
+    assert lib.e2d_adjoint_batch_destroy(None) == e2d.E2D_OK
+    J = ctypes.c_double()
+    assert lib.e2d_adjoint_batch_objective(None, 10, 0.6, 0.6, 0.1, ctypes.byref(J)) == e2d.E2D_ERR_INVALID_ARG
