@@ -135,8 +135,10 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
 }
 
 // riemann_2d_hllc (serial_ref/m_utils.f90:534-644) reverse: fb -> (qlb, qrb).
+// Also returns the forward flux (bit for bit riemann_hllc's) in flux[4].
 __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const double ql[4], const double qr[4],
-                                                 const double fb[4], double qlb[4], double qrb[4]) {
+                                                 const double fb[4], double qlb[4], double qrb[4],
+                                                 double flux[4]) {
   // ---- forward recomputation (same operations and branches as riemann_hllc)
   const double rl = O::max(ql[ID], h.smallr), rr = O::max(qr[ID], h.smallr);
   const double rlsp = rl * h.smallp, rrsp = rr * h.smallp;
@@ -171,6 +173,10 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   } else { branch = 4; ro = rr; uo = ur; ptoto = pr; etoto = etotr; }
   const double fr = ro * uo;
   const bool vleft = O::gt0(fr);
+  flux[ID] = fr;
+  flux[IU] = (fr * uo) + ptoto;
+  flux[IP] = (etoto + ptoto) * uo;
+  flux[IV] = fr * (vleft ? vl : vr);
 
   // ---- reverse
   double rlb = 0, rrb = 0, plb = 0, prb = 0, ulb = 0, urb = 0, vlb = 0, vrb = 0, etotlb = 0, etotrb = 0;

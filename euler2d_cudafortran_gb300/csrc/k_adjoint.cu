@@ -144,18 +144,21 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
       t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
     }
-    double flux[4];
-    riemann_hllc(h, ql, qr, flux);
     double rb[4];
     if (xface) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) { dtdxb += flux[v] * fb[v]; rb[v] = fb[v] * dtd; }
+      for (int v = 0; v < 4; ++v) rb[v] = fb[v] * dtd;
     } else {  // the stored y flux is the Riemann flux with IU and IV swapped back
-      dtdyb += flux[ID] * fb[ID] + flux[IP] * fb[IP] + flux[IV] * fb[IU] + flux[IU] * fb[IV];
       rb[ID] = fb[ID] * dtd; rb[IP] = fb[IP] * dtd; rb[IU] = fb[IV] * dtd; rb[IV] = fb[IU] * dtd;
     }
-    double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0};
-    adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb);
+    double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0}, flux[4];
+    adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb, flux);
+    if (xface) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) dtdxb += flux[v] * fb[v];
+    } else {
+      dtdyb += flux[ID] * fb[ID] + flux[IP] * fb[IP] + flux[IV] * fb[IU] + flux[IU] * fb[IV];
+    }
     if (!xface) {
       double t = qlb[IU]; qlb[IU] = qlb[IV]; qlb[IV] = t;
       t = qrb[IU]; qrb[IU] = qrb[IV]; qrb[IV] = t;

@@ -31,12 +31,10 @@ __device__ bool same(double x, double y) {
   return a == b;
 }
 
-// op 0: division, op 1: square root, op 2: multiplication.  Modes 0-2 as
-// rand_double; mode 4 signed zeros and small integers; mode 3 builds
+// op 0: division, op 1: square root.  Modes 0-2 as rand_double; mode 4 signed
+// zeros and small integers; mode 3 builds
 // operands whose exact result lies within one part in 2^60 of a rounding
-// boundary (quotient q + 1/2 ulp times b, or (q + 1/2 ulp)^2), and for the
-// multiplication operands of 22 and 25 significant bits, whose products are
-// exact or ties in a large fraction of cases.
+// boundary (quotient q + 1/2 ulp times b, or (q + 1/2 ulp)^2).
 __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned long long* bad, double* first) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const uint64_t r1 = mix64(seed ^ (uint64_t)k), r2 = mix64(r1 + 0x1234567ull);
@@ -49,9 +47,6 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       a = (r1 & 1) ? -a : a;
       b = rand_double(r2, (r2 & 1) ? 0 : 2);
       if (op == 1) a = (r1 & 4) ? a : (double)((r1 >> 8) & 7);
-    } else if (op == 2) {
-      a = __longlong_as_double((long long)((r1 & 0x800fffffc0000000ull) | ((uint64_t)(1000 + (r1 >> 52) % 48) << 52)));
-      b = __longlong_as_double((long long)((r2 & 0x800ffffff8000000ull) | ((uint64_t)(1000 + (r2 >> 52) % 48) << 52)));
     } else if (op == 0) {
       b = rand_double(r2, 1);
       const double q = rand_double(r1, 1);
@@ -64,8 +59,8 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       a = __dmul_rn(q + h, q + h);
       a = __longlong_as_double(__double_as_longlong(a) + (long long)(r2 & 3) - 1);
     }
-    const double x = op == 0 ? e2d::emul::div_rn(a, b) : op == 1 ? e2d::emul::sqrt_rn(a) : e2d::emul::mul_rn(a, b);
-    const double y = op == 0 ? __ddiv_rn(a, b) : op == 1 ? __dsqrt_rn(a) : __dmul_rn(a, b);
+    const double x = op == 0 ? e2d::emul::div_rn(a, b) : e2d::emul::sqrt_rn(a);
+    const double y = op == 0 ? __ddiv_rn(a, b) : __dsqrt_rn(a);
     if (!same(x, y)) {
       if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
     }
@@ -82,13 +77,6 @@ __global__ void k_rate(int op, int emulated, int iters, double* out) {
         x2 = e2d::emul::div_rn(c, x2) + 1.0; x3 = e2d::emul::div_rn(c, x3) + 1.0;
       } else {
         x0 = c / x0 + 1.0; x1 = c / x1 + 1.0; x2 = c / x2 + 1.0; x3 = c / x3 + 1.0;
-      }
-    } else if (op == 2) {
-      if (emulated) {
-        x0 = e2d::emul::mul_rn(c, x0) + 1.0; x1 = e2d::emul::mul_rn(c, x1) + 1.0;
-        x2 = e2d::emul::mul_rn(c, x2) + 1.0; x3 = e2d::emul::mul_rn(c, x3) + 1.0;
-      } else {
-        x0 = c * x0 + 1.0; x1 = c * x1 + 1.0; x2 = c * x2 + 1.0; x3 = c * x3 + 1.0;
       }
     } else {
       if (emulated) {
@@ -107,7 +95,7 @@ __global__ void k_rate(int op, int emulated, int iters, double* out) {
 extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* first_bad, double* emulated_per_s,
                                   double* native_per_s) {
-  if (op < 0 || op > 2 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
+  if ((op != 0 && op != 1) || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {

@@ -13,8 +13,7 @@
 //   (init_implode, serial_ref/m_run.f90:548).
 //
 // Every division, square root, comparison, min/max, multiplication by 0.5 or
-// 2 and sign flip goes through Ops<Real>, and every other multiplication
-// through mul<site>.  For double these run on the
+// 2 and sign flip goes through Ops<Real>.  For double these run on the
 // integer and FP32 pipes (emul64.cuh) and return the same bits as the IEEE
 // operations, which leaves the FP64 pipe -- the limit of this kernel on
 // GB300 -- to the additions and multiplications.  Building with
@@ -99,25 +98,6 @@ struct Ops<double> {
 };
 #endif
 
-// Multiplications by site.  In the FP64 build the sites selected by the bit
-// mask E2D_MUL_SITES multiply on the integer pipes (emul::mul_rn, bit for bit
-// the IEEE product) and the others on the FP64 pipe; which mix is fastest is
-// a matter of balancing the pipes, never of results.
-enum MulSite { MS_RIEMANN = 0, MS_TRACE = 1, MS_SOURCES = 2, MS_FLUX = 3, MS_PRIM = 4, MS_SLOPES = 5 };
-#ifndef E2D_MUL_SITES
-#define E2D_MUL_SITES 0x00
-#endif
-template <int SITE>
-__device__ __forceinline__ float mul(float a, float b) { return a * b; }
-template <int SITE>
-__device__ __forceinline__ double mul(double a, double b) {
-#ifdef E2D_FP64_NATIVE
-  return a * b;
-#else
-  return ((E2D_MUL_SITES >> SITE) & 1) ? emul::mul_rn(a, b) : a * b;
-#endif
-}
-
 // A pitched structure-of-arrays state: 4 planes of jsize rows of `pitch`
 // elements; element (i, j, v) (0-based) at v*plane + j*pitch + i.
 template <typename Real>
@@ -140,16 +120,16 @@ __device__ __forceinline__ void primitives(const Hydro<Real>& h, const Real u[4]
   q[ID] = O::max(u[ID], h.smallr);
   q[IU] = O::div(u[IU], q[ID]);
   q[IV] = O::div(u[IV], q[ID]);
-  const Real eken = O::half(mul<MS_PRIM>(q[IU], q[IU]) + mul<MS_PRIM>(q[IV], q[IV]));
+  const Real eken = O::half((q[IU] * q[IU]) + (q[IV] * q[IV]));
   const Real e = O::div(u[IP], q[ID]) - eken;
-  q[IP] = O::max(mul<MS_PRIM>(mul<MS_PRIM>(h.gm1, q[ID]), e), mul<MS_PRIM>(q[ID], h.smallp));
+  q[IP] = O::max((h.gm1 * q[ID]) * e, q[ID] * h.smallp);
 }
 
 // Sound speed of eos (serial_ref/m_utils.f90:27) from primitive q.
 template <typename Real>
 __device__ __forceinline__ Real sound_speed(const Hydro<Real>& h, const Real q[4]) {
   using O = Ops<Real>;
-  return O::sqrt(O::div(mul<MS_PRIM>(h.gamma0, q[IP]), q[ID]));
+  return O::sqrt(O::div(h.gamma0 * q[IP], q[ID]));
 }
 
 // The compute_dt term of one cell, serial_ref/m_run.f90:278-281.
@@ -177,7 +157,7 @@ __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm) {
   const Real drgt = mc ? O::twice(dr) : dr;
   const Real dcen = O::half(qp - qm);
   const Real slop = O::min(rabs(dlft), rabs(drgt));
-  const Real dlim = O::le0(mul<MS_SLOPES>(dlft, drgt)) ? Real(0.0) : slop;
+  const Real dlim = O::le0(dlft * drgt) ? Real(0.0) : slop;
   return O::neg_if(O::min(dlim, rabs(dcen)), !O::ge0(dcen));
 }
 
@@ -206,11 +186,10 @@ __device__ __forceinline__ void trace_sources(const Hydro<Real>& h, const Real q
                                               const Real dqy[4], Real s[4]) {
   using O = Ops<Real>;
   const Real r = q[ID], p = q[IP], u = q[IU], v = q[IV];
-  constexpr int S = MS_SOURCES;
-  s[ID] = ((-mul<S>(u, dqx[ID])) - mul<S>(v, dqy[ID])) - mul<S>(dqx[IU] + dqy[IV], r);
-  s[IP] = ((-mul<S>(u, dqx[IP])) - mul<S>(v, dqy[IP])) - mul<S>(mul<S>(dqx[IU] + dqy[IV], h.gamma0), p);
-  s[IU] = ((-mul<S>(u, dqx[IU])) - mul<S>(v, dqy[IU])) - O::div(dqx[IP], r);
-  s[IV] = ((-mul<S>(u, dqx[IV])) - mul<S>(v, dqy[IV])) - O::div(dqy[IP], r);
+  s[ID] = ((-(u * dqx[ID])) - (v * dqy[ID])) - ((dqx[IU] + dqy[IV]) * r);
+  s[IP] = ((-(u * dqx[IP])) - (v * dqy[IP])) - (((dqx[IU] + dqy[IV]) * h.gamma0) * p);
+  s[IU] = ((-(u * dqx[IU])) - (v * dqy[IU])) - O::div(dqx[IP], r);
+  s[IV] = ((-(u * dqx[IV])) - (v * dqy[IV])) - O::div(dqy[IP], r);
 }
 
 // Face state of trace_unsplit_2d_along_dir, serial_ref/m_utils.f90:218-252:
@@ -224,7 +203,7 @@ __device__ __forceinline__ void trace_face(const Hydro<Real>& h, const Real q[4]
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     const Real a = PLUS ? (q[v] + O::half(dq[v])) : (q[v] - O::half(dq[v]));
-    qf[v] = a + O::half(mul<MS_TRACE>(s[v], dtd));
+    qf[v] = a + O::half(s[v] * dtd);
   }
   qf[ID] = O::max(h.smallr, qf[ID]);
 }
@@ -233,13 +212,12 @@ __device__ __forceinline__ void trace_face(const Hydro<Real>& h, const Real q[4]
 template <typename Real>
 __device__ __forceinline__ void cmpflx(const Hydro<Real>& h, const Real qg[4], Real flux[4]) {
   using O = Ops<Real>;
-  constexpr int R = MS_RIEMANN;
-  flux[ID] = mul<R>(qg[ID], qg[IU]);
-  flux[IU] = mul<R>(flux[ID], qg[IU]) + qg[IP];
-  flux[IV] = mul<R>(flux[ID], qg[IV]);
-  const Real ekin = mul<R>(O::half(qg[ID]), mul<R>(qg[IU], qg[IU]) + mul<R>(qg[IV], qg[IV]));
-  const Real etot = mul<R>(qg[IP], h.entho) + ekin;
-  flux[IP] = mul<R>(qg[IU], etot + qg[IP]);
+  flux[ID] = qg[ID] * qg[IU];
+  flux[IU] = (flux[ID] * qg[IU]) + qg[IP];
+  flux[IV] = flux[ID] * qg[IV];
+  const Real ekin = O::half(qg[ID]) * ((qg[IU] * qg[IU]) + (qg[IV] * qg[IV]));
+  const Real etot = (qg[IP] * h.entho) + ekin;
+  flux[IP] = qg[IU] * (etot + qg[IP]);
 }
 
 // riemann_2d (two-shock approximate solver + cmpflx), serial_ref/m_utils.f90:349-492.
@@ -249,43 +227,42 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
   using O = Ops<Real>;
   const Real ONE = Real(1.0), ZERO = Real(0.0);
   const Real tol = Real(1e-6f);
-  constexpr int R = MS_RIEMANN;
   const Real rl = O::max(qleft[ID], h.smallr);
   const Real ul = qleft[IU];
-  const Real pl = O::max(qleft[IP], mul<R>(rl, h.smallp));
+  const Real pl = O::max(qleft[IP], rl * h.smallp);
   const Real rr = O::max(qright[ID], h.smallr);
   const Real ur = qright[IU];
-  const Real pr = O::max(qright[IP], mul<R>(rr, h.smallp));
-  const Real cl = mul<R>(mul<R>(h.gamma0, pl), rl);
-  const Real cr = mul<R>(mul<R>(h.gamma0, pr), rr);
+  const Real pr = O::max(qright[IP], rr * h.smallp);
+  const Real cl = (h.gamma0 * pl) * rl;
+  const Real cr = (h.gamma0 * pr) * rr;
   Real wl = O::sqrt(cl);
   Real wr = O::sqrt(cr);
-  Real pold = O::max(O::div((mul<R>(wr, pl) + mul<R>(wl, pr)) + mul<R>(mul<R>(wl, wr), ul - ur), wl + wr), ZERO);
+  Real pold = O::max(O::div(((wr * pl) + (wl * pr)) + ((wl * wr) * (ul - ur)), wl + wr), ZERO);
   Real conv = ONE;
   int iter = 0;
   while (iter < h.niter_riemann && O::gt(conv, tol)) {
-    const Real wwl = O::sqrt(mul<R>(cl, ONE + O::div(mul<R>(h.gamma6, pold - pl), pl)));
-    const Real wwr = O::sqrt(mul<R>(cr, ONE + O::div(mul<R>(h.gamma6, pold - pr), pr)));
-    const Real ql = O::div(mul<R>(mul<R>(O::twice(wwl), wwl), wwl), mul<R>(wwl, wwl) + cl);
-    const Real qr = O::div(mul<R>(mul<R>(O::twice(wwr), wwr), wwr), mul<R>(wwr, wwr) + cr);
+    const Real wwl = O::sqrt(cl * (ONE + O::div(h.gamma6 * (pold - pl), pl)));
+    const Real wwr = O::sqrt(cr * (ONE + O::div(h.gamma6 * (pold - pr), pr)));
+    const Real ql = O::div((O::twice(wwl) * wwl) * wwl, (wwl * wwl) + cl);
+    const Real qr = O::div((O::twice(wwr) * wwr) * wwr, (wwr * wwr) + cr);
     const Real usl = ul - O::div(pold - pl, wwl);
     const Real usr = ur + O::div(pold - pr, wwr);
-    const Real delp = O::max(mul<R>(O::div(mul<R>(qr, ql), qr + ql), usl - usr), -pold);
+    const Real delp = O::max(O::div(qr * ql, qr + ql) * (usl - usr), -pold);
     pold = pold + delp;
     conv = rabs(O::div(delp, pold + h.smallpp));
     iter = iter + 1;
   }
   const Real pstar = pold;
-  wl = O::sqrt(mul<R>(cl, ONE + O::div(mul<R>(h.gamma6, pstar - pl), pl)));
-  wr = O::sqrt(mul<R>(cr, ONE + O::div(mul<R>(h.gamma6, pstar - pr), pr)));
+  wl = O::sqrt(cl * (ONE + O::div(h.gamma6 * (pstar - pl), pl)));
+  wr = O::sqrt(cr * (ONE + O::div(h.gamma6 * (pstar - pr), pr)));
   const Real ustar = O::half(((ul + O::div(pl - pstar, wl)) + ur) - O::div(pr - pstar, wr));
   const bool left = O::ge0(ustar);  // sgnm = +1 (else -1)
   Real ro, uo, po, wo;
   if (left) { ro = rl; uo = ul; po = pl; wo = wl; }
   else      { ro = rr; uo = ur; po = pr; wo = wr; }
-  const Real co = O::max(h.smallc, O::sqrt(rabs(O::div(mul<R>(h.gamma0, po), ro))));
-  const Real rstar = O::max(O::div(ro, ONE + O::div(mul<R>(ro, po - pstar), mul<R>(wo, wo))), h.smallr);
-  const Real cstar = O::max(h.smallc, O::sqrt(rabs(O::div(mul<R>(h.gamma0, pstar), rstar))));
+  const Real co = O::max(h.smallc, O::sqrt(rabs(O::div(h.gamma0 * po, ro))));
+  const Real rstar = O::max(O::div(ro, ONE + O::div(ro * (po - pstar), wo * wo)), h.smallr);
+  const Real cstar = O::max(h.smallc, O::sqrt(rabs(O::div(h.gamma0 * pstar, rstar))));
   const Real suo = O::neg_if(uo, !left), sust = O::neg_if(ustar, !left);  // sgnm*uo, sgnm*ustar
   Real spout = co - suo;
   Real spin = cstar - sust;
@@ -294,9 +271,9 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
   const Real scr = O::max(spout - spin, h.smallc + rabs(spout + spin));
   const Real frac = O::half(ONE + O::div(spout + spin, scr));
   Real qg[4];
-  qg[ID] = mul<R>(frac, rstar) + mul<R>(ONE - frac, ro);
-  qg[IU] = mul<R>(frac, ustar) + mul<R>(ONE - frac, uo);
-  qg[IP] = mul<R>(frac, pstar) + mul<R>(ONE - frac, po);
+  qg[ID] = (frac * rstar) + ((ONE - frac) * ro);
+  qg[IU] = (frac * ustar) + ((ONE - frac) * uo);
+  qg[IP] = (frac * pstar) + ((ONE - frac) * po);
   if (O::lt0(spout)) { qg[ID] = ro; qg[IU] = uo; qg[IP] = po; }
   if (O::gt0(spin)) { qg[ID] = rstar; qg[IU] = ustar; qg[IP] = pstar; }
   qg[IV] = left ? qleft[IV] : qright[IV];
@@ -308,52 +285,49 @@ template <typename Real>
 __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real qleft[4],
                                              const Real qright[4], Real flux[4]) {
   using O = Ops<Real>;
-  constexpr int R = MS_RIEMANN;
   const Real rl = O::max(qleft[ID], h.smallr);
-  const Real pl = O::max(qleft[IP], mul<R>(rl, h.smallp));
+  const Real pl = O::max(qleft[IP], rl * h.smallp);
   const Real ul = qleft[IU];
   const Real hrl = O::half(rl);
-  Real ecinl = mul<R>(mul<R>(hrl, ul), ul);
-  ecinl = ecinl + mul<R>(mul<R>(hrl, qleft[IV]), qleft[IV]);
-  const Real etotl = mul<R>(pl, h.entho) + ecinl;
+  Real ecinl = (hrl * ul) * ul;
+  ecinl = ecinl + ((hrl * qleft[IV]) * qleft[IV]);
+  const Real etotl = (pl * h.entho) + ecinl;
   const Real ptotl = pl;
   const Real rr = O::max(qright[ID], h.smallr);
-  const Real pr = O::max(qright[IP], mul<R>(rr, h.smallp));
+  const Real pr = O::max(qright[IP], rr * h.smallp);
   const Real ur = qright[IU];
   const Real hrr = O::half(rr);
-  Real ecinr = mul<R>(mul<R>(hrr, ur), ur);
-  ecinr = ecinr + mul<R>(mul<R>(hrr, qright[IV]), qright[IV]);
-  const Real etotr = mul<R>(pr, h.entho) + ecinr;
+  Real ecinr = (hrr * ur) * ur;
+  ecinr = ecinr + ((hrr * qright[IV]) * qright[IV]);
+  const Real etotr = (pr * h.entho) + ecinr;
   const Real ptotr = pr;
-  const Real cfastl = O::sqrt(O::max(O::div(mul<R>(h.gamma0, pl), rl), h.smallc2));
-  const Real cfastr = O::sqrt(O::max(O::div(mul<R>(h.gamma0, pr), rr), h.smallc2));
+  const Real cfastl = O::sqrt(O::max(O::div(h.gamma0 * pl, rl), h.smallc2));
+  const Real cfastr = O::sqrt(O::max(O::div(h.gamma0 * pr, rr), h.smallc2));
   const Real cmax = O::max(cfastl, cfastr);
   const Real SL = O::min(ul, ur) - cmax;
   const Real SR = O::max(ul, ur) + cmax;
-  const Real rcl = mul<R>(rl, ul - SL);
-  const Real rcr = mul<R>(rr, SR - ur);
-  const Real ustar = O::div((mul<R>(rcr, ur) + mul<R>(rcl, ul)) + (ptotl - ptotr), rcr + rcl);
-  const Real ptotstar =
-      O::div((mul<R>(rcr, ptotl) + mul<R>(rcl, ptotr)) + mul<R>(mul<R>(rcl, rcr), ul - ur), rcr + rcl);
+  const Real rcl = rl * (ul - SL);
+  const Real rcr = rr * (SR - ur);
+  const Real ustar = O::div(((rcr * ur) + (rcl * ul)) + (ptotl - ptotr), rcr + rcl);
+  const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
   Real ro, uo, ptoto, etoto;
   if (O::gt0(SL)) {
     ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
   } else if (O::gt0(ustar)) {
-    ro = O::div(mul<R>(rl, SL - ul), SL - ustar);
+    ro = O::div(rl * (SL - ul), SL - ustar);
     uo = ustar; ptoto = ptotstar;
-    etoto = O::div((mul<R>(SL - ul, etotl) - mul<R>(ptotl, ul)) + mul<R>(ptotstar, ustar), SL - ustar);
+    etoto = O::div((((SL - ul) * etotl) - (ptotl * ul)) + (ptotstar * ustar), SL - ustar);
   } else if (O::gt0(SR)) {
-    ro = O::div(mul<R>(rr, SR - ur), SR - ustar);
+    ro = O::div(rr * (SR - ur), SR - ustar);
     uo = ustar; ptoto = ptotstar;
-    etoto = O::div((mul<R>(SR - ur, etotr) - mul<R>(ptotr, ur)) + mul<R>(ptotstar, ustar), SR - ustar);
+    etoto = O::div((((SR - ur) * etotr) - (ptotr * ur)) + (ptotstar * ustar), SR - ustar);
   } else {
     ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
   }
-  const Real mflux = mul<R>(ro, uo);
-  flux[ID] = mflux;
-  flux[IU] = mul<R>(mflux, uo) + ptoto;
-  flux[IP] = mul<R>(etoto + ptoto, uo);
-  flux[IV] = O::gt0(flux[ID]) ? mul<R>(flux[ID], qleft[IV]) : mul<R>(flux[ID], qright[IV]);
+  flux[ID] = ro * uo;
+  flux[IU] = ((ro * uo) * uo) + ptoto;
+  flux[IP] = (etoto + ptoto) * uo;
+  flux[IV] = O::gt0(flux[ID]) ? (flux[ID] * qleft[IV]) : (flux[ID] * qright[IV]);
 }
 
 template <typename Real>

@@ -124,7 +124,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         trace_face<Real, false>(h, qc, dq, s, dtdx, qr);
         riemann(h, ql, qr, flux);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = mul<MS_FLUX>(flux[v], dtdx);
+        for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = flux[v] * dtdx;
       }
     } else if (k < NF) {
       const int kk = k - NXF;
@@ -143,7 +143,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         riemann(h, ql, qr, flux);
         t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sfy[(v * (TY + 1) + g) * TX + c] = mul<MS_FLUX>(flux[v], dtdy);
+        for (int v = 0; v < 4; ++v) sfy[(v * (TY + 1) + g) * TX + c] = flux[v] * dtdy;
       }
     }
   }

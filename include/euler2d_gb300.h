@@ -134,12 +134,10 @@ int e2d_time_steps(e2d_run* h, int nStep0, int nsteps, float* ms);
  * the FP64 step.  Not part of the reference; used by the benchmark. */
 int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
 
-/* Self-test of the library's integer-pipe double division (op 0), square
- * root (op 1) and multiplication (op 2) against the hardware operations on n
- * seeded inputs (mode 0 any bit pattern, 1 exponents near 1, 2 exponents
- * within +-400, 3 results next to rounding boundaries or, for the
- * multiplication, exact products and ties, 4 signed zeros and small
- * integers): *mismatches counts results that differ in any bit,
+/* Self-test of the library's integer-pipe double division (op 0) and square
+ * root (op 1) against the hardware operations on n seeded inputs (mode 0 any
+ * bit pattern, 1 exponents near 1, 2 exponents within +-400, 3 results next to
+ * rounding boundaries, 4 signed zeros and small integers): *mismatches counts results that differ in any bit,
  * first_bad[4] (optional) = a, b, emulated, hardware of the first one; the
  * two rates (optional) are chained operations per second.  Not part of the
  * reference; used by the tests. */

@@ -1,19 +1,19 @@
-"""The integer-pipe double division, square root and multiplication used by
-the FP64 step must agree bit for bit with the hardware IEEE operations."""
+"""The integer-pipe double division and square root used by the FP64 step
+must agree bit for bit with the hardware IEEE operations."""
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4], ids=["any-bits", "near-1", "wide", "near-boundary", "zeros"])
-@pytest.mark.parametrize("op", [0, 1, 2], ids=["div", "sqrt", "mul"])
+@pytest.mark.parametrize("op", [0, 1], ids=["div", "sqrt"])
 def test_emulated_matches_hardware(e2d, op, mode):
     bad, first, _ = e2d.selftest_arith(op, mode, 1 << 26, seed=12345 + 17 * mode + op)
     assert bad == 0, f"{bad} mismatches; first (a, b, emulated, hardware) = {first}"
 
 
 def test_emulated_rates_reported(e2d):
-    for op in (0, 1, 2):
+    for op in (0, 1):
         bad, _, (em, na) = e2d.selftest_arith(op, 1, 1 << 20, seed=7, rates=True)
         assert bad == 0 and em > 0 and na > 0
         print(f"op {op}: emulated {em / 1e9:.1f} G/s, hardware {na / 1e9:.1f} G/s")
