@@ -242,7 +242,9 @@ def run_reference(a, dist):
 def measure_batched(E, a):
     """64 seeded problems (sides 128..1024, offsets, states and walls at random)
     advanced together by one launch per step from a captured graph, against the
-    same problems advanced one after another with the single-run kernel."""
+    same problems advanced one after another: with the single-run kernel's
+    device-resident graphs (plain) and with the reference's per-call loop
+    (compute_dt with dt read back, then godunov_unsplit, every step)."""
     from euler2d_cudafortran_gb300.ensemble import diagonal_ensemble
     ens = diagonal_ensemble(64, 12345)
     n = a.batched_steps
@@ -260,6 +262,7 @@ def measure_batched(E, a):
         batched_ms = b.last_advance_ms()
         health = [b.health(k) for k in range(b.nprob)]
     plain_ms = 0.0
+    percall_s = 0.0
     for k, (nx, ny) in enumerate(ens.sizes):
         bc = ens.bcs[k]
         p = E.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=riemann, precision=a.precision,
@@ -269,13 +272,28 @@ def measure_batched(E, a):
             run.init_diagonal(*(x[k] for x in init))
             run.advance(0, n, log=False)
             plain_ms += run.last_advance_ms()
+            # the reference's own loop (serial_ref/main.f90:66-74): compute_dt
+            # with dt back on the host, then godunov_unsplit, every step
+            run.init_diagonal(*(x[k] for x in init))
+            run.synchronize()
+            t0 = time.perf_counter()
+            run.compute_dt(0)
+            run.make_boundaries(0)
+            for step in range(n):
+                dt = run.compute_dt(step % 2)
+                run.godunov_unsplit(step, dt)
+            run.synchronize()
+            percall_s += time.perf_counter() - t0
     cells = ens.cells
     return {"workload": f"64 problems, sides uniform in {{128..1024 step 64}} (total {cells} cells), "
                         f"seed 12345, {n} steps per graph", "steps": n,
             "mcells_per_s": round(cells * n / (batched_ms * 1e-3) / 1e6, 2),
             "plain_problem_by_problem_mcells_per_s": round(cells * n / (plain_ms * 1e-3) / 1e6, 2),
             "speedup_vs_problem_by_problem": round(plain_ms / batched_ms, 3),
+            "percall_problem_by_problem_mcells_per_s": round(cells * n / percall_s / 1e6, 2),
+            "speedup_vs_percall_problem_by_problem": round(percall_s * 1e3 / batched_ms, 3),
             "batched_ms": round(batched_ms, 3), "plain_ms": round(plain_ms, 3),
+            "percall_ms": round(percall_s * 1e3, 3),
             "schedule": sched, "autotune_s": round(tune_s, 2), "health_flags_nonzero": int(sum(1 for h in health if h))}
 
 
