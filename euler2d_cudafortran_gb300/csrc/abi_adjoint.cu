@@ -43,8 +43,8 @@ struct e2d_adjoint {
   double* part_v = nullptr;
   long long* part_i = nullptr;
   int nparts = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr, join = nullptr;
   float last_forward_ms = 0, last_gradient_ms = 0;
   std::map<std::tuple<int, int, double, double, double>, cudaGraphExec_t> graphs;
 };
@@ -77,13 +77,14 @@ void free_buffers(e2d_adjoint* a) {
   a->cap_steps = 0;
 }
 
-// Buffers for nsteps: 2 ping-pong states, ceil(N/K) checkpoints, K segment states.
+// Buffers for nsteps: 2 ping-pong states, ceil(N/K) checkpoints, and two
+// sets of K segment states (one being reversed while the next is recomputed).
 int ensure(e2d_adjoint* a, int nsteps) {
   if (nsteps <= a->cap_steps) return E2D_OK;
   free_buffers(a);
   const int K = std::max(1, (int)std::ceil(std::sqrt((double)nsteps)));
   const int nchk = (nsteps + K - 1) / K;
-  const int nstates = 2 + nchk + K;
+  const int nstates = 2 + nchk + 2 * K;
   if (cudaMalloc(&a->pool, (size_t)nstates * a->state_elems * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&a->dt_log, nsteps * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&a->inv_log, nsteps * sizeof(double)) != cudaSuccess ||
@@ -105,10 +106,11 @@ int ensure(e2d_adjoint* a, int nsteps) {
 
 constexpr int kPing = 0;  // states 0, 1: forward ping-pong
 int chk_index(const e2d_adjoint*, int s) { return 2 + s; }
-int seg_index(const e2d_adjoint* a, int k) { return 2 + a->nchk + k; }
+int seg_index(const e2d_adjoint* a, int set, int k) { return 2 + a->nchk + set * a->kseg + k; }
 
-// Forward N steps from state 0 (u) with checkpoints; J (and, with the seed,
-// Ubar_N = dJ/dU_N) on the device.  Enqueued only: no host synchronisation.
+// Forward N steps from state 0 (u); J on the device and, for a gradient,
+// checkpoints every K steps and the seed Ubar_N = dJ/dU_N.  Enqueued only:
+// no host synchronisation.
 void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double sig, bool with_adjoint_seed,
                      const double* dt_fixed) {
   const Hydro<double>& h = a->h;
@@ -118,7 +120,7 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
   launch_boundaries<double>(h, state(a, kPing), s);            // main.f90:46
   for (int k = 0; k < nsteps; ++k) {
     const int in = k & 1, out = in ^ 1;
-    if (k % a->kseg == 0)
+    if (with_adjoint_seed && k % a->kseg == 0)  // checkpoints only for the reverse sweep
       cudaMemcpyAsync(state(a, chk_index(a, k / a->kseg)).p, state(a, in).p, a->state_elems * sizeof(double),
                       cudaMemcpyDeviceToDevice, s);
     const int rd = k & 1;
@@ -138,37 +140,52 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
   launch_objective(h, state(a, nsteps & 1), xc, yc, sig, a->J, seed, s);
 }
 
-// The reverse sweep: segments last first, each recomputed from its
-// checkpoint with the logged dt, then reversed step by step.  The running
-// CFL maximum's rises are found on the device from the logged maxima.
-// Leaves dJ/dU_0 in ub[final_ub(a, nsteps)].
+// Recomputes segment sg's states (k0 .. k1-1) into segment set `set` from
+// its checkpoint, with the logged dt (bit for bit the forward states).
+void enqueue_recompute(e2d_adjoint* a, int sg, int set, int nsteps, cudaStream_t s) {
+  const Hydro<double>& h = a->h;
+  const int K = a->kseg, k0 = sg * K, k1 = std::min(k0 + K, nsteps);
+  cudaMemcpyAsync(state(a, seg_index(a, set, 0)).p, state(a, chk_index(a, sg)).p, a->state_elems * sizeof(double),
+                  cudaMemcpyDeviceToDevice, s);
+  launch_seg_corners(h, a->pool, a->state_elems, a->pitch, a->plane, kPing, seg_index(a, set, 0), k0, k1 - k0, s);
+  for (int m = k0; m < k1 - 1; ++m) {
+    StepDt<double> sd;
+    sd.dt_value = 0.0;
+    sd.dt_ptr = a->dt_log + m;
+    sd.from_slot = 0;
+    sd.rd_slot = -1;
+    sd.wr_slot = -1;
+    sd.dt_log = nullptr;
+    sd.log_index = 0;
+    launch_fused_map<double>(h, a->maps[seg_index(a, set, m - k0)], state(a, seg_index(a, set, m - k0)),
+                             state(a, seg_index(a, set, m - k0 + 1)), sd, a->ctl, true, s);
+  }
+}
+
+// The reverse sweep: segments last first.  Segment sg is reversed on the
+// main stream from segment set sg & 1 while segment sg - 1 is recomputed on
+// the second stream into the other set, so the two overlap on the GPU.  The
+// running CFL maximum's rises are found on the device from the logged
+// maxima.  Leaves dJ/dU_0 in ub[final_ub(nsteps)].
 void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
   const Hydro<double>& h = a->h;
-  cudaStream_t s = a->stream;
+  cudaStream_t s = a->stream, s2 = a->stream2;
   cudaMemsetAsync(a->dtbar_log, 0, nsteps * sizeof(double), s);
   int cur = 0;  // ub[cur] holds Ubar of the state after the step being reversed
-  const int K = a->kseg;
-  for (int sg = (nsteps + K - 1) / K - 1; sg >= 0; --sg) {
-    const int k0 = sg * K, k1 = std::min(k0 + K, nsteps);
-    cudaMemcpyAsync(state(a, seg_index(a, 0)).p, state(a, chk_index(a, sg)).p, a->state_elems * sizeof(double),
-                    cudaMemcpyDeviceToDevice, s);
-    launch_seg_corners(h, a->pool, a->state_elems, a->pitch, a->plane, kPing, seg_index(a, 0), k0, k1 - k0, s);
-    for (int m = k0; m < k1 - 1; ++m) {  // recompute the segment's states with the logged dt
-      StepDt<double> sd;
-      sd.dt_value = 0.0;
-      sd.dt_ptr = a->dt_log + m;
-      sd.from_slot = 0;
-      sd.rd_slot = -1;
-      sd.wr_slot = -1;
-      sd.dt_log = nullptr;
-      sd.log_index = 0;
-      launch_fused_map<double>(h, a->maps[seg_index(a, m - k0)], state(a, seg_index(a, m - k0)),
-                               state(a, seg_index(a, m - k0 + 1)), sd, a->ctl, true, s);
+  const int K = a->kseg, last = (nsteps + K - 1) / K - 1;
+  enqueue_recompute(a, last, last & 1, nsteps, s);
+  for (int sg = last; sg >= 0; --sg) {
+    const int set = sg & 1, k0 = sg * K, k1 = std::min(k0 + K, nsteps);
+    if (sg > 0) {  // the other set is free once segment sg + 1 has been reversed
+      cudaEventRecord(a->fork, s);
+      cudaStreamWaitEvent(s2, a->fork, 0);
+      enqueue_recompute(a, sg - 1, set ^ 1, nsteps, s2);
+      cudaEventRecord(a->join, s2);
     }
     for (int m = k1 - 1; m >= k0; --m) {
       const int nxt = cur ^ 1;
       cudaMemsetAsync(a->ub[nxt], 0, a->state_elems * sizeof(double), s);
-      Field<double> um = state(a, seg_index(a, m - k0));
+      Field<double> um = state(a, seg_index(a, set, m - k0));
       launch_step_rev(h, um, ubf(a, cur), ubf(a, nxt), a->dt_log + m, a->dtbar_log + m, s);
       if (dt_mode == 1) {
         launch_argmax(h, um, a->part_v, a->part_i, a->nparts, a->inv_log, m, s);
@@ -177,6 +194,7 @@ void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
       }
       cur = nxt;
     }
+    if (sg > 0) cudaStreamWaitEvent(s, a->join, 0);  // segment sg - 1 recomputed
   }
 }
 
@@ -237,8 +255,10 @@ int e2d_adjoint_create(const e2d_params* p, e2d_adjoint** out) {
     return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint state failed");
   }
   if (cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&a->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&a->e0) != cudaSuccess || cudaEventCreate(&a->e1) != cudaSuccess ||
-      cudaEventCreate(&a->e2) != cudaSuccess || step_rev_setup() != 0) {
+      cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->join, cudaEventDisableTiming) != cudaSuccess || step_rev_setup() != 0) {
     e2d_adjoint_destroy(a);
     return afail(E2D_ERR_CUDA, "stream/event/kernel setup failed");
   }
@@ -259,7 +279,12 @@ int e2d_adjoint_destroy(e2d_adjoint* a) {
   cudaFree(a->part_i);
   if (a->e0) cudaEventDestroy(a->e0);
   if (a->e1) cudaEventDestroy(a->e1);
-  if (a->e2) cudaEventDestroy(a->e2);
+  if (a->fork) cudaEventDestroy(a->fork);
+  if (a->join) cudaEventDestroy(a->join);
+  if (a->stream2) {
+    cudaStreamSynchronize(a->stream2);
+    cudaStreamDestroy(a->stream2);
+  }
   if (a->stream) cudaStreamDestroy(a->stream);
   delete a;
   return E2D_OK;

@@ -11,8 +11,10 @@
 // pair of one call is a single captured CUDA graph, replayed on later calls
 // with the same step count, dt mode and objective.  Buffers of a problem
 // (indices into its slab): 0, 1 forward ping-pong; 2.. checkpoints every
-// K = ceil(sqrt(N)) steps; then K segment states; then 2 adjoint states.  The
-// initial state lives in its own array so that a call can be replayed.
+// K = ceil(sqrt(N)) steps; then two sets of K segment states (a segment is
+// reversed on the main stream from one set while the next is recomputed on a
+// second stream into the other); then 2 adjoint states.  The initial state
+// lives in its own array so that a call can be replayed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,7 +45,7 @@ struct e2d_adjoint_batch {
   int kseg = 0, nchk = 0, cap_steps = 0;
   AdjProb* d_probs = nullptr;          // by problem index
   BatchProb<double>* d_fwd = nullptr;  // forward ping-pong, work-list order
-  BatchProb<double>* d_seg = nullptr;  // [K - 1][nprob]: segment j -> j + 1
+  BatchProb<double>* d_seg = nullptr;  // [2][K - 1][nprob]: segment set, state j -> j + 1
   int fwd_tiles = 0, fwd_grid = 0, rev_tiles = 0, nparts = 64;
   Ctl* ctls = nullptr;
   double *dt_log = nullptr, *inv_log = nullptr, *dtbar_log = nullptr;
@@ -51,8 +53,8 @@ struct e2d_adjoint_batch {
   double* part_v = nullptr;
   long long* part_i = nullptr;
   double* grad = nullptr;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr, join = nullptr;
   float last_forward_ms = 0, last_gradient_ms = 0;
   std::map<std::tuple<int, int, int, double, double, double>, cudaGraphExec_t> graphs;
 };
@@ -69,7 +71,7 @@ int abfail(int code, const std::string& m) { return set_error(code, m); }
 
 constexpr int kPing = 0, kChk = 2;
 int seg_base(const e2d_adjoint_batch* b) { return kChk + b->nchk; }
-int ub_base(const e2d_adjoint_batch* b) { return kChk + b->nchk + b->kseg; }
+int ub_base(const e2d_adjoint_batch* b) { return kChk + b->nchk + 2 * b->kseg; }
 int nbuf(const e2d_adjoint_batch* b) { return ub_base(b) + 2; }
 
 void clear_graphs(e2d_adjoint_batch* b) {
@@ -127,7 +129,7 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
   if (cudaMalloc(&b->slab, total * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&b->d_probs, sizeof(AdjProb) * b->nprob) != cudaSuccess ||
       cudaMalloc(&b->d_fwd, sizeof(BatchProb<double>) * b->nprob) != cudaSuccess ||
-      cudaMalloc(&b->d_seg, sizeof(BatchProb<double>) * b->nprob * std::max(1, K - 1)) != cudaSuccess ||
+      cudaMalloc(&b->d_seg, sizeof(BatchProb<double>) * b->nprob * 2 * std::max(1, K - 1)) != cudaSuccess ||
       cudaMalloc(&b->dt_log, nlog * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&b->inv_log, nlog * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&b->dtbar_log, nlog * sizeof(double)) != cudaSuccess) {
@@ -164,7 +166,8 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return (long long)b->params[x].nx * b->params[x].ny > (long long)b->params[y].nx * b->params[y].ny;
   });
-  std::vector<BatchProb<double>> fw(b->nprob), sg((size_t)b->nprob * std::max(1, K - 1));
+  const size_t nseg_arr = (size_t)b->nprob * std::max(1, K - 1);
+  std::vector<BatchProb<double>> fw(b->nprob), sg(2 * nseg_arr);
   int ft = 0;
   for (int k = 0; k < b->nprob; ++k) {
     const int p = order[k];
@@ -179,12 +182,13 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
     F.tile_begin = ft;
     F.id = p;
     ft += F.ntx * F.nty;
-    for (int j = 0; j + 1 < K; ++j) {
-      BatchProb<double>& S = sg[(size_t)j * b->nprob + k];
-      S = F;
-      S.u = ap[p].base + (size_t)(seg_base(b) + j) * b->se[p];
-      S.u2 = ap[p].base + (size_t)(seg_base(b) + j + 1) * b->se[p];
-    }
+    for (int set = 0; set < 2; ++set)
+      for (int j = 0; j + 1 < K; ++j) {
+        BatchProb<double>& S = sg[set * nseg_arr + (size_t)j * b->nprob + k];
+        S = F;
+        S.u = ap[p].base + (size_t)(seg_base(b) + set * K + j) * b->se[p];
+        S.u2 = ap[p].base + (size_t)(seg_base(b) + set * K + j + 1) * b->se[p];
+      }
   }
   b->fwd_tiles = ft;
   int sms = 0;
@@ -249,21 +253,38 @@ void enqueue_forward(e2d_adjoint_batch* b, int nsteps, double xc, double yc, dou
   launch_batch_objective(B, kPing + (nsteps & 1), xc, yc, sig, adjoint ? ub_base(b) : -1, s);
 }
 
-// Reverse sweep; dJ/dU_0 ends in buffer ub_base + (nsteps & 1).
+// Recomputes segment sg of every problem into segment set `set` from its
+// checkpoint with the logged dt.
+void enqueue_recompute(e2d_adjoint_batch* b, int sg, int set, int nsteps, cudaStream_t s) {
+  const AdjBatch B = view(b);
+  const int K = b->kseg, k0 = sg * K, k1 = std::min(k0 + K, nsteps), sb = seg_base(b) + set * K;
+  launch_batch_copy(B, kChk + sg, sb, s);
+  launch_batch_seg_corners(B, kPing, sb, k0, k1 - k0, s);
+  const size_t nseg_arr = (size_t)b->nprob * std::max(1, K - 1);
+  for (int m = k0; m < k1 - 1; ++m) {
+    BatchLaunch<double> L = step_launch(b, b->d_seg + set * nseg_arr + (size_t)(m - k0) * b->nprob);
+    L.dt_src = b->dt_log + (size_t)m * b->nprob;
+    launch_batch_step<double>(0, L, s);
+  }
+}
+
+// Reverse sweep, segment sg from set sg & 1 on the main stream while segment
+// sg - 1 is recomputed into the other set on the second stream; dJ/dU_0 ends
+// in buffer ub_base + (nsteps & 1).
 void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
-  cudaStream_t s = b->stream;
+  cudaStream_t s = b->stream, s2 = b->stream2;
   const AdjBatch B = view(b);
   cudaMemsetAsync(b->dtbar_log, 0, sizeof(double) * nsteps * b->nprob, s);
-  const int K = b->kseg, sb = seg_base(b), ub = ub_base(b);
+  const int K = b->kseg, ub = ub_base(b), last = (nsteps + K - 1) / K - 1;
   int cur = 0;
-  for (int sg = (nsteps + K - 1) / K - 1; sg >= 0; --sg) {
-    const int k0 = sg * K, k1 = std::min(k0 + K, nsteps);
-    launch_batch_copy(B, kChk + sg, sb, s);
-    launch_batch_seg_corners(B, kPing, sb, k0, k1 - k0, s);
-    for (int m = k0; m < k1 - 1; ++m) {  // recompute the segment with the logged dt
-      BatchLaunch<double> L = step_launch(b, b->d_seg + (size_t)(m - k0) * b->nprob);
-      L.dt_src = b->dt_log + (size_t)m * b->nprob;
-      launch_batch_step<double>(0, L, s);
+  enqueue_recompute(b, last, last & 1, nsteps, s);
+  for (int sg = last; sg >= 0; --sg) {
+    const int set = sg & 1, k0 = sg * K, k1 = std::min(k0 + K, nsteps), sb = seg_base(b) + set * K;
+    if (sg > 0) {
+      cudaEventRecord(b->fork, s);
+      cudaStreamWaitEvent(s2, b->fork, 0);
+      enqueue_recompute(b, sg - 1, set ^ 1, nsteps, s2);
+      cudaEventRecord(b->join, s2);
     }
     for (int m = k1 - 1; m >= k0; --m) {
       const int nxt = cur ^ 1;
@@ -275,6 +296,7 @@ void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
       }
       cur = nxt;
     }
+    if (sg > 0) cudaStreamWaitEvent(s, b->join, 0);
   }
   launch_batch_extract(B, ub + cur, b->grad, s);
 }
@@ -387,8 +409,10 @@ int e2d_adjoint_batch_create(const e2d_params* base, int nprob, const int* nx, c
     return cleanup(E2D_ERR_OOM, "cudaMalloc of the batched adjoint state failed");
   }
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess ||
-      batch_step_rev_setup() != 0)
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess || batch_step_rev_setup() != 0)
     return cleanup(E2D_ERR_CUDA, "stream/event/kernel setup failed");
   cudaMemsetAsync(b->u0, 0, u0_total * sizeof(double), b->stream);
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return cleanup(E2D_ERR_CUDA, "initialisation failed");
@@ -409,6 +433,12 @@ int e2d_adjoint_batch_destroy(e2d_adjoint_batch* b) {
   cudaFree(b->grad);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->stream2) {
+    cudaStreamSynchronize(b->stream2);
+    cudaStreamDestroy(b->stream2);
+  }
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return E2D_OK;

@@ -6,10 +6,12 @@
 // its box (primitives, slopes, trace sources), then for each face it owns
 // (the left / lower faces of its cells, plus the last wall faces) forms the
 // flux adjoint from the update (F_i enters cell i with + and cell i-1 with -),
-// runs the Riemann, trace, source, slope and primitive reverses, and scatters
-// the result into shared accumulators; ghost-cell adjoints are folded back to
-// the interior cells make_boundaries copied them from (serial_ref/m_run.f90:
-// 561-648).  The 2x2 ghost corners are constants and receive nothing.
+// runs the Riemann, trace, source, slope and primitive reverses, and adds the
+// results into shared memory in passes where no two threads touch the same
+// word (no shared atomics); ghost-cell adjoints are folded back to the
+// interior cells make_boundaries copied them from (serial_ref/m_run.f90:
+// 561-648) with global atomic adds, since neighbouring tiles overlap there.
+// The 2x2 ghost corners are constants and receive nothing.
 #include "adjoint.cuh"
 #include "adjoint_launch.h"
 #include "tile.cuh"
@@ -31,10 +33,6 @@ constexpr int RA_OFF = UB_OFF + 4 * NUB;        // ring adj.  dqx[4] dqy[4] s[4]
 constexpr int QB_OFF = RA_OFF + 12 * NRING;     // q adjoint  [4][ABY][ABX]
 constexpr int N_SMEM = QB_OFF + 4 * NBOX;
 constexpr size_t SMEM_BYTES = (size_t)N_SMEM * sizeof(double) + 64;
-
-__device__ __forceinline__ void sadd(double* p, double x) {
-  if (x != 0.0) atomicAdd(p, x);
-}
 
 // One 32 x 7 tile (bx, by) of the reverse step; sm is the dynamic shared area.
 __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
@@ -102,87 +100,104 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     const int x = i - (i0 - 1), y = j - (j0 - 1);
     return (x >= 0 && x <= ATX && y >= 0 && y <= ATY) ? sub[(v * (ATY + 1) + y) * (ATX + 1) + x] : 0.0;
   };
-  constexpr int NXF = (ATX + 1) * ATY, NYF = ATX * (ATY + 1);
-  for (int k = tid; k < NXF + NYF; k += ANT) {
-    const bool xface = k < NXF;
-    int a, b;  // ring indices of the two cells (left/lower, right/upper)
-    int ia, ja;
+  // Faces in four passes -- x faces with even, then odd f; y faces with even,
+  // then odd g -- so that no two faces of a pass touch the same cell and the
+  // adjoints are added into shared memory without atomics.  A pass has at
+  // most ANT faces: one per thread.
+  constexpr int NFX_EVEN = ATX / 2 + 1, NFX_ODD = (ATX + 1) / 2;       // f in [0, ATX]
+  constexpr int NGY_EVEN = ATY / 2 + 1, NGY_ODD = (ATY + 1) / 2;       // g in [0, ATY]
+  static_assert(NFX_EVEN * ATY <= ANT && NGY_EVEN * ATX <= ANT, "one face per thread per pass");
+#pragma unroll 1
+  for (int pass = 0; pass < 4; ++pass) {
+    const bool xface = pass < 2;
+    const int par = pass & 1;
+    const int nfx = par ? NFX_ODD : NFX_EVEN;
+    const int nf = xface ? nfx * ATY : (par ? NGY_ODD : NGY_EVEN) * ATX;
+    int a = 0, b = 0;  // ring indices of the two cells (left/lower, right/upper)
+    int ia = 0, ja = 0;
     double fb[4];
+    bool valid = tid < nf;
     if (xface) {
-      const int f = k % (ATX + 1), r = k / (ATX + 1);
+      const int f = 2 * (tid % nfx) + par, r = tid / nfx;
       const int i = i0 + f, j = j0 + r;
-      if (!(i <= h.nx + 2 && j <= h.ny + 1 && (f < ATX || i == h.nx + 2))) continue;
+      valid = valid && i <= h.nx + 2 && j <= h.ny + 1 && (f < ATX || i == h.nx + 2);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) fb[v] = UB(v, i, j) - UB(v, i - 1, j);
+      for (int v = 0; v < 4; ++v) fb[v] = valid ? UB(v, i, j) - UB(v, i - 1, j) : 0.0;
       a = (r + 1) * ARX + f;
       b = a + 1;
       ia = f + 1; ja = r + 2;  // box coordinates of the left cell
     } else {
-      const int kk = k - NXF;
-      const int c = kk % ATX, g = kk / ATX;
+      const int c = tid % ATX, g = 2 * (tid / ATX) + par;
       const int i = i0 + c, j = j0 + g;
-      if (!(i <= h.nx + 1 && j <= h.ny + 2 && (g < ATY || j == h.ny + 2))) continue;
+      valid = valid && i <= h.nx + 1 && j <= h.ny + 2 && (g < ATY || j == h.ny + 2);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) fb[v] = UB(v, i, j) - UB(v, i, j - 1);
+      for (int v = 0; v < 4; ++v) fb[v] = valid ? UB(v, i, j) - UB(v, i, j - 1) : 0.0;
       a = g * ARX + (c + 1);
       b = a + ARX;
       ia = c + 2; ja = g + 1;  // box coordinates of the lower cell
     }
-    const double dtd = xface ? dtdx : dtdy;
-    const int nrm = xface ? 0 : 4;  // slope block of the face normal
-    double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], ql[4], qr[4];
+    if (valid) {
+      const double dtd = xface ? dtdx : dtdy;
+      const int nrm = xface ? 0 : 4;  // slope block of the face normal
+      double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], ql[4], qr[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      qa[v] = Q(v, ja, ia);
-      qb_[v] = xface ? Q(v, ja, ia + 1) : Q(v, ja + 1, ia);
-      dqa[v] = sdq[(nrm + v) * NRING + a]; dqb[v] = sdq[(nrm + v) * NRING + b];
-      sa[v] = ss[v * NRING + a]; sb[v] = ss[v * NRING + b];
-    }
-    trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
-    trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
-    if (!xface) {
-      double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
-      t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
-    }
-    double rb[4];
-    if (xface) {
+      for (int v = 0; v < 4; ++v) {
+        qa[v] = Q(v, ja, ia);
+        qb_[v] = xface ? Q(v, ja, ia + 1) : Q(v, ja + 1, ia);
+        dqa[v] = sdq[(nrm + v) * NRING + a]; dqb[v] = sdq[(nrm + v) * NRING + b];
+        sa[v] = ss[v * NRING + a]; sb[v] = ss[v * NRING + b];
+      }
+      trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
+      trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
+      if (!xface) {
+        double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
+        t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
+      }
+      double rb[4];
+      if (xface) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) rb[v] = fb[v] * dtd;
-    } else {  // the stored y flux is the Riemann flux with IU and IV swapped back
-      rb[ID] = fb[ID] * dtd; rb[IP] = fb[IP] * dtd; rb[IU] = fb[IV] * dtd; rb[IV] = fb[IU] * dtd;
-    }
-    double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0}, flux[4];
-    adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb, flux);
-    if (xface) {
+        for (int v = 0; v < 4; ++v) rb[v] = fb[v] * dtd;
+      } else {  // the stored y flux is the Riemann flux with IU and IV swapped back
+        rb[ID] = fb[ID] * dtd; rb[IP] = fb[IP] * dtd; rb[IU] = fb[IV] * dtd; rb[IV] = fb[IU] * dtd;
+      }
+      double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0}, flux[4];
+      adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb, flux);
+      if (xface) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) dtdxb += flux[v] * fb[v];
-    } else {
-      dtdyb += flux[ID] * fb[ID] + flux[IP] * fb[IP] + flux[IV] * fb[IU] + flux[IU] * fb[IV];
-    }
-    if (!xface) {
-      double t = qlb[IU]; qlb[IU] = qlb[IV]; qlb[IV] = t;
-      t = qrb[IU]; qrb[IU] = qrb[IV]; qrb[IV] = t;
-    }
-    double qab[4] = {0, 0, 0, 0}, dqab[4] = {0, 0, 0, 0}, sab[4] = {0, 0, 0, 0};
-    double qbb[4] = {0, 0, 0, 0}, dqbb[4] = {0, 0, 0, 0}, sbb[4] = {0, 0, 0, 0};
-    double& dtdb = xface ? dtdxb : dtdyb;
-    adj::trace_face_rev<true>(h, qa, dqa, sa, dtd, qlb, qab, dqab, sab, dtdb);
-    adj::trace_face_rev<false>(h, qb_, dqb, sb, dtd, qrb, qbb, dqbb, sbb, dtdb);
-    const int ka = ja * ABX + ia;
-    const int kb = xface ? ka + 1 : ka + ABX;
+        for (int v = 0; v < 4; ++v) dtdxb += flux[v] * fb[v];
+      } else {
+        dtdyb += flux[ID] * fb[ID] + flux[IP] * fb[IP] + flux[IV] * fb[IU] + flux[IU] * fb[IV];
+      }
+      if (!xface) {
+        double t = qlb[IU]; qlb[IU] = qlb[IV]; qlb[IV] = t;
+        t = qrb[IU]; qrb[IU] = qrb[IV]; qrb[IV] = t;
+      }
+      double qab[4] = {0, 0, 0, 0}, dqab[4] = {0, 0, 0, 0}, sab[4] = {0, 0, 0, 0};
+      double qbb[4] = {0, 0, 0, 0}, dqbb[4] = {0, 0, 0, 0}, sbb[4] = {0, 0, 0, 0};
+      double& dtdb = xface ? dtdxb : dtdyb;
+      adj::trace_face_rev<true>(h, qa, dqa, sa, dtd, qlb, qab, dqab, sab, dtdb);
+      adj::trace_face_rev<false>(h, qb_, dqb, sb, dtd, qrb, qbb, dqbb, sbb, dtdb);
+      const int ka = ja * ABX + ia;
+      const int kb = xface ? ka + 1 : ka + ABX;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      sadd(&sqb[v * NBOX + ka], qab[v]);
-      sadd(&sqb[v * NBOX + kb], qbb[v]);
-      sadd(&sra[(nrm + v) * NRING + a], dqab[v]);
-      sadd(&sra[(nrm + v) * NRING + b], dqbb[v]);
-      sadd(&sra[(8 + v) * NRING + a], sab[v]);
-      sadd(&sra[(8 + v) * NRING + b], sbb[v]);
+      for (int v = 0; v < 4; ++v) {
+        sqb[v * NBOX + ka] += qab[v];
+        sqb[v * NBOX + kb] += qbb[v];
+        sra[(nrm + v) * NRING + a] += dqab[v];
+        sra[(nrm + v) * NRING + b] += dqbb[v];
+        sra[(8 + v) * NRING + a] += sab[v];
+        sra[(8 + v) * NRING + b] += sbb[v];
+      }
     }
+    __syncthreads();
   }
-  __syncthreads();
 
-  // ---- ring cells: sources and slopes reverse
+  // ---- ring cells: sources and slopes reverse.  A ring cell adds its own
+  // (centre) adjoint to its box cell and leaves the adjoints of its four
+  // limiter neighbours in its own slots -- east in the dq_x adjoint, west in
+  // the dq_y adjoint, north in the source adjoint, south in the source
+  // values, none of which anyone else reads now -- so no two threads write
+  // the same word; the box pass below gathers them.
   const bool mc = h.slope_type == 2;
   const bool lim = h.slope_type == 1 || h.slope_type == 2;
   for (int k = tid; k < NRING; k += ANT) {
@@ -204,16 +219,20 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
         adj::slope1_rev(mc, qc[v], Q(v, y, x + 1), Q(v, y, x - 1), dqxb[v], qcb[v], qe, qw);
         adj::slope1_rev(mc, qc[v], Q(v, y + 1, x), Q(v, y - 1, x), dqyb[v], qcb[v], qn, qs);
       }
-      sadd(&sqb[v * NBOX + kc], qcb[v]);
-      sadd(&sqb[v * NBOX + kc + 1], qe);
-      sadd(&sqb[v * NBOX + kc - 1], qw);
-      sadd(&sqb[v * NBOX + kc + ABX], qn);
-      sadd(&sqb[v * NBOX + kc - ABX], qs);
+      sqb[v * NBOX + kc] += qcb[v];
+      sra[v * NRING + k] = qe;
+      sra[(4 + v) * NRING + k] = qw;
+      sra[(8 + v) * NRING + k] = qn;
+      ss[v * NRING + k] = qs;
     }
   }
   __syncthreads();
 
-  // ---- box cells: primitives reverse, fold ghosts back, identity part of the update
+  // ---- box cells: gather the limiter neighbours' adjoints, primitives
+  // reverse, fold ghosts back, identity part of the update
+  auto ring_of = [&](int x, int y) -> int {  // ring index of box cell (x, y), -1 if not a ring cell
+    return (x >= 1 && x <= ARX && y >= 1 && y <= ARY) ? (y - 1) * ARX + (x - 1) : -1;
+  };
   for (int k = tid; k < NBOX; k += ANT) {
     const int y = k / ABX, x = k - y * ABX;
     const int gi = i0 - GW + x, gj = j0 - GW + y;
@@ -221,9 +240,18 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     const bool xin = gi >= GW && gi <= h.nx + 1, yin = gj >= GW && gj <= h.ny + 1;
     if (!xin && !yin) continue;  // corner: a constant
     double qb[4], u[4], ub[4] = {0, 0, 0, 0};
+    const int rw = ring_of(x - 1, y), re = ring_of(x + 1, y), rs = ring_of(x, y - 1), rn = ring_of(x, y + 1);
     bool any = false;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) { qb[v] = sqb[v * NBOX + k]; any |= qb[v] != 0.0; }
+    for (int v = 0; v < 4; ++v) {
+      double t = sqb[v * NBOX + k];
+      if (rw >= 0) t += sra[v * NRING + rw];          // west neighbour's east adjoint
+      if (re >= 0) t += sra[(4 + v) * NRING + re];    // east neighbour's west adjoint
+      if (rs >= 0) t += sra[(8 + v) * NRING + rs];    // south neighbour's north adjoint
+      if (rn >= 0) t += ss[v * NRING + rn];           // north neighbour's south adjoint
+      qb[v] = t;
+      any |= t != 0.0;
+    }
     if (any) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) u[v] = un.at(v, gj, gi);
