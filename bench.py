@@ -60,7 +60,7 @@ def parse_args():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-nx", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=200)
-    ap.add_argument("--adjoint-batch-steps", type=int, default=100)
+    ap.add_argument("--adjoint-batch-steps", type=int, default=100, help="0 skips the batched adjoint")
     return ap.parse_args()
 
 
@@ -467,7 +467,8 @@ def run_ours(a, dist):
     adjoint = adjoint_batch = None
     if dist.rank == 0 and not a.no_adjoint:
         adjoint = measure_adjoint(E, a)
-        adjoint_batch = measure_adjoint_batch(E, a)
+        if a.adjoint_batch_steps > 0:
+            adjoint_batch = measure_adjoint_batch(E, a)
 
     if dist.rank == 0:
         isz = a.nx + 4

@@ -48,7 +48,8 @@ EXPORTED_SYMBOLS = [
     "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
     "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
-    "e2d_godunov_unsplit_noalloc", "e2d_selftest_arith",
+    "e2d_godunov_unsplit_noalloc", "e2d_selftest_arith", "e2d_begin_download", "e2d_wait_download",
+    "e2d_host_alloc", "e2d_host_free",
     "e2d_batch_create", "e2d_batch_destroy", "e2d_batch_init_diagonal", "e2d_batch_upload_state",
     "e2d_batch_download_state", "e2d_batch_advance", "e2d_batch_last_advance_ms", "e2d_batch_set_schedule",
     "e2d_batch_get_schedule", "e2d_batch_tune", "e2d_batch_get_health",
@@ -116,6 +117,10 @@ def load_library(path: str = LIB_PATH):
         "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
                              ctypes.POINTER(ctypes.c_size_t)],
         "e2d_godunov_unsplit_noalloc": [ctypes.POINTER(Params), vp, vp, ctypes.c_size_t, d, vp],
+        "e2d_begin_download": [vp, i, vp],
+        "e2d_wait_download": [vp],
+        "e2d_host_alloc": [ctypes.c_size_t, ctypes.POINTER(vp)],
+        "e2d_host_free": [vp],
         "e2d_selftest_arith": [i, i, ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong),
                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double)],
@@ -238,6 +243,19 @@ class HydroRun:
         a = self.new_state()
         _check(self._lib.e2d_download_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
         return a
+
+    def begin_download(self, which: int, out: np.ndarray):
+        """Starts an asynchronous copy of state `which` into `out` (see
+        e2d_begin_download); call wait_download() before reading `out`."""
+        if out.shape != self.new_state().shape or out.dtype != self.dtype or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous state array of this run")
+        self._pending_out = out
+        _check(self._lib.e2d_begin_download(self._h, which, out.ctypes.data_as(ctypes.c_void_p)))
+
+    def wait_download(self) -> np.ndarray | None:
+        _check(self._lib.e2d_wait_download(self._h))
+        out, self._pending_out = getattr(self, "_pending_out", None), None
+        return out
 
     # -- the reference procedures -----------------------------------------
     def compute_dt(self, useU: int) -> float:

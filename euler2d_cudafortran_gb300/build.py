@@ -77,7 +77,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs)
     drv = [os.path.join(DRIVER, f) for f in DRIVER_SOURCES]
     if all(os.path.exists(d) for d in drv) and _stale(EXE, drv + [LIB, os.path.join(DRIVER, "namelist.h")]):
-        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-o", EXE]
+        _run(["g++", "-O2", "-std=c++17", "-pthread", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-o", EXE]
              + drv + ["-L", OUT, "-leuler2d_gb300", "-Wl,-rpath,$ORIGIN"])
     return LIB
 

@@ -64,6 +64,12 @@ struct e2d_run {
   // folded[b]: the running CFL maximum (slot cur_slot) already includes the
   // current state of buffer b (0 = u, 1 = u2), so compute_dt on it needs no sweep.
   bool folded[2] = {false, false};
+  // asynchronous output: a device snapshot of one state, copied to the host
+  // on its own stream while later steps run on `stream`
+  void* snapshot = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
+  bool download_pending = false;
 };
 
 namespace {
@@ -287,6 +293,13 @@ int e2d_destroy(e2d_run* r) {
   cudaFree(r->dt_log);
   if (r->ev0) cudaEventDestroy(r->ev0);
   if (r->ev1) cudaEventDestroy(r->ev1);
+  if (r->copy_stream) {
+    cudaStreamSynchronize(r->copy_stream);
+    cudaStreamDestroy(r->copy_stream);
+  }
+  if (r->ev_snap) cudaEventDestroy(r->ev_snap);
+  if (r->ev_copied) cudaEventDestroy(r->ev_copied);
+  cudaFree(r->snapshot);
   if (r->own_stream) cudaStreamDestroy(r->own_stream);
   delete r;
   return E2D_OK;
@@ -357,6 +370,61 @@ int e2d_download_state(e2d_run* r, int which, void* host) {
   E2D_CK(cudaMemcpy2DAsync(host, w, which ? r->u2 : r->u, r->pitch * r->es, w, (size_t)4 * r->jsize,
                            cudaMemcpyDeviceToHost, r->stream));
   E2D_CK(cudaStreamSynchronize(r->stream));
+  return E2D_OK;
+}
+
+int e2d_begin_download(e2d_run* r, int which, void* host) {
+  if (int rc = check_run(r)) return rc;
+  if (!host || (which != 0 && which != 1)) return fail(E2D_ERR_INVALID_ARG, "bad download arguments");
+  if (int rc = use_device(r)) return rc;
+  if (!r->snapshot) {
+    if (cudaMalloc(&r->snapshot, state_dev_bytes(r)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(E2D_ERR_OOM, "cudaMalloc of the output snapshot failed");
+    }
+    E2D_CK(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+    E2D_CK(cudaEventCreateWithFlags(&r->ev_snap, cudaEventDisableTiming));
+    E2D_CK(cudaEventCreateWithFlags(&r->ev_copied, cudaEventDisableTiming));
+  }
+  if (r->download_pending) E2D_CK(cudaEventSynchronize(r->ev_copied));  // the snapshot is reused
+  // snapshot in stream order (device to device), then to the host on the copy stream
+  E2D_CK(cudaMemcpyAsync(r->snapshot, which ? r->u2 : r->u, state_dev_bytes(r), cudaMemcpyDeviceToDevice,
+                         r->stream));
+  E2D_CK(cudaEventRecord(r->ev_snap, r->stream));
+  E2D_CK(cudaStreamWaitEvent(r->copy_stream, r->ev_snap, 0));
+  const size_t w = (size_t)r->isize * r->es;
+  E2D_CK(cudaMemcpy2DAsync(host, w, r->snapshot, r->pitch * r->es, w, (size_t)4 * r->jsize, cudaMemcpyDeviceToHost,
+                           r->copy_stream));
+  E2D_CK(cudaEventRecord(r->ev_copied, r->copy_stream));
+  r->download_pending = true;
+  return E2D_OK;
+}
+
+int e2d_wait_download(e2d_run* r) {
+  if (int rc = check_run(r)) return rc;
+  if (!r->download_pending) return E2D_OK;
+  if (int rc = use_device(r)) return rc;
+  E2D_CK(cudaEventSynchronize(r->ev_copied));
+  r->download_pending = false;
+  return E2D_OK;
+}
+
+int e2d_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr || bytes == 0) return fail(E2D_ERR_INVALID_ARG, "bad host allocation arguments");
+  *ptr = nullptr;
+  if (cudaMallocHost(ptr, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return fail(E2D_ERR_OOM, "cudaMallocHost failed");
+  }
+  return E2D_OK;
+}
+
+int e2d_host_free(void* ptr) {
+  if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(E2D_ERR_CUDA, "cudaFreeHost failed");
+  }
   return E2D_OK;
 }
 

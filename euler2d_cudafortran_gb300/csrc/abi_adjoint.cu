@@ -124,8 +124,8 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
       cudaMemcpyAsync(state(a, chk_index(a, k / a->kseg)).p, state(a, in).p, a->state_elems * sizeof(double),
                       cudaMemcpyDeviceToDevice, s);
     const int rd = k & 1;
-    cudaMemcpyAsync(a->inv_log + k, inv_slot<double>(a->ctl, rd), sizeof(double), cudaMemcpyDeviceToDevice, s);
     StepDt<double> sd;
+    sd.inv_log = a->inv_log;
     sd.dt_value = dt_fixed ? dt_fixed[k] : 0.0;
     sd.dt_ptr = nullptr;
     sd.from_slot = dt_fixed ? 0 : 1;

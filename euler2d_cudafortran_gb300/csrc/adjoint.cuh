@@ -59,7 +59,7 @@ __device__ __forceinline__ void cell_invdt_rev(const Hydro<double>& h, const dou
   const double cb = O::div(tb, h.dx) + O::div(tb, h.dy);
   qb[IU] = O::neg_if(O::div(tb, h.dx), !O::ge0(q[IU]));
   qb[IV] = O::neg_if(O::div(tb, h.dy), !O::ge0(q[IV]));
-  const double c2b = O::div(cb, 2.0 * c);
+  const double c2b = O::div(cb, O::twice(c));
   qb[IP] += O::div(c2b * h.gamma0, q[ID]);
   qb[ID] -= O::div(c2b * c2, q[ID]);
   primitives_rev(h, u, qb, ub);
@@ -74,7 +74,6 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
   const double drgt = mc ? O::twice(dr) : dr;
   const double dcen = O::half(qp - qm);
   if (O::le0(dlft * drgt)) return;  // limited to zero
-  const double st = mc ? 2.0 : 1.0;
   const bool neg = !O::ge0(dcen);   // dsgn = -1
   const double al = fabs(dlft), ar = fabs(drgt), ac = fabs(dcen);
   const bool use_l = picks_first_min(al, ar);
@@ -83,13 +82,14 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
     // slope = dsgn * |dlft| or dsgn * |drgt|
     const double x = use_l ? dlft : drgt;
     const double g = ((!O::ge0(x)) != neg) ? -sb : sb;  // dsgn * sign(x) * sb
-    if (use_l) { qbar += st * g; qmbar -= st * g; }
-    else { qpbar += st * g; qbar -= st * g; }
+    const double sg = mc ? O::twice(g) : g;              // st * g, st = 2 (MC) or 1
+    if (use_l) { qbar += sg; qmbar -= sg; }
+    else { qpbar += sg; qbar -= sg; }
   } else {
     // slope = dsgn * |dcen| = dcen
-    const double g = ((!O::ge0(dcen)) != neg) ? -sb : sb;
-    qpbar += 0.5 * g;
-    qmbar -= 0.5 * g;
+    const double g = O::half(((!O::ge0(dcen)) != neg) ? -sb : sb);
+    qpbar += g;
+    qmbar -= g;
   }
 }
 
@@ -127,10 +127,11 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
   if (emul::gt_i(h.smallr, raw)) qfb[ID] = 0.0;
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
+    const double hq = O::half(qfb[v]);
     qb[v] += qfb[v];
-    dqb[v] += PLUS ? 0.5 * qfb[v] : -0.5 * qfb[v];
-    sb[v] += 0.5 * dtd * qfb[v];
-    dtdb += 0.5 * s[v] * qfb[v];
+    dqb[v] += PLUS ? hq : -hq;
+    sb[v] += dtd * hq;
+    dtdb += s[v] * hq;
   }
 }
 
@@ -236,21 +237,22 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   if (min_l) ulb += SLb; else urb += SLb;
   const double cfastlb = cmax_l ? cmaxb : 0.0, cfastrb = cmax_l ? 0.0 : cmaxb;
   if (cl_act) {
-    const double cab = O::div(cfastlb, 2.0 * cfastl);
+    const double cab = O::div(cfastlb, O::twice(cfastl));
     plb += O::div(cab * h.gamma0, rl);
     rlb -= O::div(cab * cal, rl);
   }
   if (cr_act) {
-    const double cab = O::div(cfastrb, 2.0 * cfastr);
+    const double cab = O::div(cfastrb, O::twice(cfastr));
     prb += O::div(cab * h.gamma0, rr);
     rrb -= O::div(cab * car, rr);
   }
   // etot = p entho + hr u u + hr v v, hr = rho / 2
   plb += etotlb * h.entho; prb += etotrb * h.entho;
-  rlb += 0.5 * etotlb * (ul * ul + vl * vl);
-  rrb += 0.5 * etotrb * (ur * ur + vr * vr);
-  ulb += etotlb * 2.0 * hrl * ul; vlb += etotlb * 2.0 * hrl * vl;
-  urb += etotrb * 2.0 * hrr * ur; vrb += etotrb * 2.0 * hrr * vr;
+  rlb += O::half(etotlb) * (ul * ul + vl * vl);
+  rrb += O::half(etotrb) * (ur * ur + vr * vr);
+  const double erl = etotlb * rl, err = etotrb * rr;  // 2 hr = rho
+  ulb += erl * ul; vlb += erl * vl;
+  urb += err * ur; vrb += err * vr;
   // pressure and density floors
   if (picks_first_max(ql[IP], rlsp)) qlb[IP] += plb; else rlb += plb * h.smallp;
   if (picks_first_max(qr[IP], rrsp)) qrb[IP] += prb; else rrb += prb * h.smallp;

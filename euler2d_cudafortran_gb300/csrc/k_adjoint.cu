@@ -20,7 +20,15 @@ namespace e2d {
 
 namespace {
 
-constexpr int ATX = 32, ATY = 7, ANT = 128;
+// Reverse tile: 32 x E2D_REV_TY cells, 128 threads, E2D_REV_MINB CTAs per SM
+// (shared memory and registers must allow that many).
+#ifndef E2D_REV_TY
+#define E2D_REV_TY 7
+#endif
+#ifndef E2D_REV_MINB
+#define E2D_REV_MINB 2
+#endif
+constexpr int ATX = 32, ATY = E2D_REV_TY, ANT = 128;
 constexpr int ABX = ATX + 4, ABY = ATY + 4, ARX = ATX + 2, ARY = ATY + 2;
 constexpr int NBOX = ABX * ABY, NRING = ARX * ARY;
 constexpr int NUB = (ATX + 1) * (ATY + 1);
@@ -298,7 +306,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   }
 }
 
-__global__ void __launch_bounds__(ANT, 2)
+__global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, const double* dt,
                double* dtbar) {
   extern __shared__ double sm[];
@@ -453,7 +461,7 @@ __device__ __forceinline__ Field<double> afield(const AdjProb& P, int k) {
 
 // Reverse step m of every problem: one CTA per 32 x 7 tile of the flattened
 // tile list (problem p owns tiles [tile_begin, tile_begin + ntx * nty)).
-__global__ void __launch_bounds__(ANT, 2)
+__global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_batch_step_rev(const AdjProb* __restrict__ probs, int nprob, const double* dt_log, double* dtbar_log, int un,
                      int ub_in, int ub_out, int m) {
   extern __shared__ double sm[];

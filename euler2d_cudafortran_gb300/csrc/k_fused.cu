@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? 2 : 3)
   if (tid == 0) {
     if (blockIdx.x == 0 && blockIdx.y == 0) {
       if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
+      if (sd.inv_log && sd.rd_slot >= 0) sd.inv_log[sd.log_index] = *inv_slot<Real>(ctl, sd.rd_slot);
       if (!isfinite(dt)) atomicOr(&ctl->health, 1u);
     }
     if (want_dt) {

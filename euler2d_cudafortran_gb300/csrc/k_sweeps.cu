@@ -209,6 +209,7 @@ template <typename Real>
 __device__ __forceinline__ void log_dt(const Hydro<Real>& h, const StepDt<Real>& sd, Ctl* ctl, Real dt) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
+    if (sd.inv_log && sd.rd_slot >= 0) sd.inv_log[sd.log_index] = *inv_slot<Real>(ctl, sd.rd_slot);
     if (!isfinite(dt)) atomicOr(&ctl->health, 1u);
   }
 }

@@ -34,6 +34,7 @@ struct StepDt {
   int wr_slot;      // slot receiving max(inv[rd], max over the new state); -1: no reduction
   Real* dt_log;     // device; may be null
   int log_index;
+  Real* inv_log = nullptr;  // device; if set, receives inv[rd_slot] (the running max this step's dt uses)
 };
 
 // ---- abi.cu ----

@@ -1,6 +1,6 @@
 // main.cpp -- the HydroRun driver of serial_ref/main.f90 on the GB300 library.
 //
-//   euler2d_gb300 test.nml [--percall] [--binary-vtk] [--no-io] [--outdir DIR]
+//   euler2d_gb300 test.nml [--percall] [--binary-vtk] [--no-io] [--sync-io] [--outdir DIR]
 //
 // Same sequence as serial_ref/main.f90:36-95: read the namelist, print the
 // parameters, init_implode, initial compute_dt, make_boundaries, then the
@@ -11,11 +11,17 @@
 // Between two outputs the steps run on the device without host round trips
 // (e2d_advance); --percall calls compute_dt + godunov_unsplit every step as
 // the reference does.  Both give the same states and dt sequence.
+//
+// Output is asynchronous unless --sync-io: the state is snapshotted on the
+// device in stream order, copied to pinned host memory on a copy stream and
+// written to its VTK file by a writer thread, while the next steps run; the
+// "io time" is then the time the step loop waits for output.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "euler2d_gb300.h"
@@ -42,11 +48,12 @@ int die(const char* what, int rc) {
 
 int main(int argc, char** argv) {
   std::string nml, outdir = ".";
-  bool percall = false, binary = false, no_io = false, parse_only = false;
+  bool percall = false, binary = false, no_io = false, parse_only = false, sync_io = false;
   for (int k = 1; k < argc; ++k) {
     if (!std::strcmp(argv[k], "--percall")) percall = true;
     else if (!std::strcmp(argv[k], "--binary-vtk")) binary = true;
     else if (!std::strcmp(argv[k], "--no-io")) no_io = true;
+    else if (!std::strcmp(argv[k], "--sync-io")) sync_io = true;
     else if (!std::strcmp(argv[k], "--parse-only")) parse_only = true;
     else if (!std::strcmp(argv[k], "--outdir") && k + 1 < argc) outdir = argv[++k];
     else nml = argv[k];
@@ -90,7 +97,9 @@ int main(int argc, char** argv) {
   if (rc) return die("init_implode", rc);
   size_t state_bytes = 0;
   e2d_get_sizes(run, nullptr, nullptr, &state_bytes);
-  std::vector<unsigned char> host(state_bytes);
+  std::vector<unsigned char> host(sync_io ? state_bytes : 0);
+  void* pinned = nullptr;
+  if (!sync_io && (rc = e2d_host_alloc(state_bytes, &pinned))) return die("host_alloc", rc);
 
   double dtd = 0;
   float dtf = 0;
@@ -107,12 +116,24 @@ int main(int argc, char** argv) {
   total.start();
   int nStep = 0;
   const double t = 0.0;  // never advanced (serial_ref/main.f90:53)
+  std::thread writer;
+  int writer_rc = 0;
   auto output = [&](int which, int step) -> int {
     io.start();
-    int r = e2d_download_state(run, which, host.data());
-    if (!r && !no_io) {
-      if (save_vtk(outdir, step, host.data(), p.nx, p.ny, p.precision, !binary).empty())
+    int r = 0;
+    if (sync_io) {
+      r = e2d_download_state(run, which, host.data());
+      if (!r && !no_io && save_vtk(outdir, step, host.data(), p.nx, p.ny, p.precision, !binary).empty())
         std::fprintf(stderr, "cannot write VTK output in %s\n", outdir.c_str());
+    } else {
+      if (writer.joinable()) writer.join();  // the previous file is written, the buffer free
+      r = writer_rc ? writer_rc : e2d_begin_download(run, which, pinned);
+      if (!r)
+        writer = std::thread([&, step]() {
+          writer_rc = e2d_wait_download(run);
+          if (!writer_rc && !no_io && save_vtk(outdir, step, pinned, p.nx, p.ny, p.precision, !binary).empty())
+            std::fprintf(stderr, "cannot write VTK output in %s\n", outdir.c_str());
+        });
     }
     io.stop();
     return r;
@@ -143,8 +164,15 @@ int main(int argc, char** argv) {
   std::printf(" Output results at step %d dt %.17g\n", nStep, dt_value());
   // serial_ref/main.f90:81 always writes u (stale after an odd number of steps)
   if ((rc = output(0, nStep))) return die("download_state", rc);
+  if (writer.joinable()) {
+    io.start();
+    writer.join();
+    io.stop();
+  }
+  if (writer_rc) return die("wait_download", writer_rc);
   e2d_synchronize(run);
   total.stop();
+  e2d_host_free(pinned);
   unsigned health = 0;
   e2d_get_health(run, &health);
   e2d_destroy(run);

@@ -147,6 +147,19 @@ int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed, u
 /* Current running maximum of 1/dt (double, whatever the precision). */
 int e2d_get_invdt(e2d_run* h, double* invdt);
 
+/* Asynchronous output (serial_ref/m_run.f90:653-720 writes the state
+ * synchronously): e2d_begin_download copies state `which` (0 = u, 1 = u2)
+ * into a device snapshot in stream order, after the steps already issued,
+ * then to `host` (Fortran layout) on a separate copy stream, and returns;
+ * steps issued afterwards run while the transfer proceeds.  `host` should
+ * come from e2d_host_alloc (pinned) for the copy to overlap.  The snapshot is
+ * reused: a second e2d_begin_download first waits for the previous copy.
+ * e2d_wait_download blocks until the last copy has landed in `host`. */
+int e2d_begin_download(e2d_run* h, int which, void* host);
+int e2d_wait_download(e2d_run* h);
+int e2d_host_alloc(size_t bytes, void** ptr);
+int e2d_host_free(void* ptr);
+
 /* Health flags accumulated by the kernels since the last call (cleared on read). */
 int e2d_get_health(e2d_run* h, unsigned* flags);
 

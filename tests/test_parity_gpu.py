@@ -66,6 +66,27 @@ def test_small_grids_bitwise(e2d, oracle, case, version, riemann, mode):
     assert_same(gpu, ref, dts, dts_ref, f"v{version} riemann={riemann} {mode}")
 
 
+TINY = [
+    dict(nx=2, ny=2, nsteps=9, bc=(1, 1, 1, 1)),
+    dict(nx=3, ny=2, nsteps=9, bc=(2, 3, 1, 2)),
+    dict(nx=2, ny=5, nsteps=9, bc=(3, 3, 3, 3)),
+    dict(nx=300, ny=3, nsteps=15, bc=(1, 2, 3, 1)),
+    dict(nx=3, ny=200, nsteps=15, bc=(2, 1, 1, 3)),
+]
+
+
+@pytest.mark.parametrize("case", TINY, ids=lambda c: f"{c['nx']}x{c['ny']}-bc{''.join(map(str, c['bc']))}")
+@pytest.mark.parametrize("version", [0, 1, 2])
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+def test_minimal_and_skinny_grids_bitwise(e2d, oracle, case, version, prec):
+    """The smallest grid the reference allows (one ghost source cell for
+    several ghosts) and grids a few cells wide, where every tile is partial."""
+    pe, po = _params(e2d, oracle, case, version, 2, prec)
+    ref, dts_ref, _, _ = oracle.run(po, case["nsteps"], prec="f64" if prec == 8 else "f32", nthreads=NTHREADS)
+    gpu, dts = e2d.run_steps(case["nsteps"], pe)
+    assert_same(gpu, ref, dts, dts_ref, f"v{version} prec={prec}")
+
+
 @pytest.mark.parametrize("riemann", [2, 0], ids=["hllc", "approx"])
 def test_plain_256_500_steps(e2d, oracle, riemann):
     """The plain-method case: 256x256, FP64, gamma 1.4, CFL 0.8, MC slopes,
