@@ -239,15 +239,22 @@ class HydroRun:
             raise ValueError(f"state must have shape (4, {self.jsize}, {self.isize})")
         _check(self._lib.e2d_upload_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
 
-    def get_state(self, which: int) -> np.ndarray:
-        a = self.new_state()
+    def get_state(self, which: int, out: np.ndarray | None = None) -> np.ndarray:
+        """State `which` (0 = u, 1 = u2) in Fortran layout; into `out` (e.g. a
+        pinned buffer) when given."""
+        if out is None:
+            a = self.new_state()
+        else:
+            if out.shape != (4, self.jsize, self.isize) or out.dtype != self.dtype or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("out must be a C-contiguous state array of this run")
+            a = out
         _check(self._lib.e2d_download_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
         return a
 
     def begin_download(self, which: int, out: np.ndarray):
         """Starts an asynchronous copy of state `which` into `out` (see
         e2d_begin_download); call wait_download() before reading `out`."""
-        if out.shape != self.new_state().shape or out.dtype != self.dtype or not out.flags["C_CONTIGUOUS"]:
+        if out.shape != (4, self.jsize, self.isize) or out.dtype != self.dtype or not out.flags["C_CONTIGUOUS"]:
             raise ValueError("out must be a C-contiguous state array of this run")
         self._pending_out = out
         _check(self._lib.e2d_begin_download(self._h, which, out.ctypes.data_as(ctypes.c_void_p)))
