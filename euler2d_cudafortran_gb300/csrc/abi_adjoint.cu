@@ -118,11 +118,17 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
   cudaMemsetAsync(a->ctl, 0, sizeof(Ctl), s);
   launch_dt_reduce<double>(h, state(a, kPing), a->ctl, 0, s);  // main.f90:42
   launch_boundaries<double>(h, state(a, kPing), s);            // main.f90:46
+  const int K = a->kseg, last = (nsteps + K - 1) / K - 1;
   for (int k = 0; k < nsteps; ++k) {
     const int in = k & 1, out = in ^ 1;
-    if (with_adjoint_seed && k % a->kseg == 0)  // checkpoints only for the reverse sweep
-      cudaMemcpyAsync(state(a, chk_index(a, k / a->kseg)).p, state(a, in).p, a->state_elems * sizeof(double),
-                      cudaMemcpyDeviceToDevice, s);
+    if (with_adjoint_seed) {  // checkpoints, and the last segment's states kept whole, for the reverse sweep
+      if (k >= last * K)
+        cudaMemcpyAsync(state(a, seg_index(a, last & 1, k - last * K)).p, state(a, in).p,
+                        a->state_elems * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      else if (k % K == 0)
+        cudaMemcpyAsync(state(a, chk_index(a, k / K)).p, state(a, in).p, a->state_elems * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s);
+    }
     const int rd = k & 1;
     StepDt<double> sd;
     sd.inv_log = a->inv_log;
@@ -164,7 +170,8 @@ void enqueue_recompute(e2d_adjoint* a, int sg, int set, int nsteps, cudaStream_t
 
 // The reverse sweep: segments last first.  Segment sg is reversed on the
 // main stream from segment set sg & 1 while segment sg - 1 is recomputed on
-// the second stream into the other set, so the two overlap on the GPU.  The
+// the second stream into the other set, so the two overlap on the GPU; the
+// last segment needs no recomputation (the forward sweep kept its states).  The
 // running CFL maximum's rises are found on the device from the logged
 // maxima.  Leaves dJ/dU_0 in ub[final_ub(nsteps)].
 void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
@@ -173,7 +180,7 @@ void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
   cudaMemsetAsync(a->dtbar_log, 0, nsteps * sizeof(double), s);
   int cur = 0;  // ub[cur] holds Ubar of the state after the step being reversed
   const int K = a->kseg, last = (nsteps + K - 1) / K - 1;
-  enqueue_recompute(a, last, last & 1, nsteps, s);
+  // the last segment's states were kept by the forward sweep
   for (int sg = last; sg >= 0; --sg) {
     const int set = sg & 1, k0 = sg * K, k1 = std::min(k0 + K, nsteps);
     if (sg > 0) {  // the other set is free once segment sg + 1 has been reversed

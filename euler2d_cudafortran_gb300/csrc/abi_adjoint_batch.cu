@@ -239,8 +239,12 @@ void enqueue_forward(e2d_adjoint_batch* b, int nsteps, double xc, double yc, dou
     launch_dt_reduce<double>(b->hd[p], u, &b->ctls[p], 0, s);  // main.f90:42
     launch_boundaries<double>(b->hd[p], u, s);                 // main.f90:46
   }
+  const int K = b->kseg, last = (nsteps + K - 1) / K - 1;
   for (int k = 0; k < nsteps; ++k) {
-    if (adjoint && k % b->kseg == 0) launch_batch_copy(B, kPing + (k & 1), kChk + k / b->kseg, s);
+    if (adjoint) {  // checkpoints, and the last segment's states kept whole, for the reverse sweep
+      if (k >= last * K) launch_batch_copy(B, kPing + (k & 1), seg_base(b) + (last & 1) * K + (k - last * K), s);
+      else if (k % K == 0) launch_batch_copy(B, kPing + (k & 1), kChk + k / K, s);
+    }
     BatchLaunch<double> L = step_launch(b, b->d_fwd);
     L.parity = k & 1;
     L.rd = k & 1;
@@ -277,7 +281,7 @@ void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
   cudaMemsetAsync(b->dtbar_log, 0, sizeof(double) * nsteps * b->nprob, s);
   const int K = b->kseg, ub = ub_base(b), last = (nsteps + K - 1) / K - 1;
   int cur = 0;
-  enqueue_recompute(b, last, last & 1, nsteps, s);
+  // the last segment's states were kept by the forward sweep
   for (int sg = last; sg >= 0; --sg) {
     const int set = sg & 1, k0 = sg * K, k1 = std::min(k0 + K, nsteps), sb = seg_base(b) + set * K;
     if (sg > 0) {

@@ -198,10 +198,10 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
     case 4: rrb += rob; urb += uob; prb += ptotob; etotrb += etotob; break;
     case 2: {
       ustarb += uob; ptotstarb += ptotob;
-      double db = -O::div(rob * ro, d) - O::div(etotob * etoto, d);
       const double rq = O::div(rob, d);
       rlb += rq * (SL - ul); SLb += rq * rl; ulb -= rq * rl;
       const double nEb = O::div(etotob, d);
+      const double db = -(rq * ro + nEb * etoto);  // d(ro, etoto)/d(d)
       SLb += nEb * etotl; ulb -= nEb * etotl; etotlb += nEb * (SL - ul);
       plb -= nEb * ul; ulb -= nEb * pl; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
       SLb += db; ustarb -= db;
@@ -209,10 +209,10 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
     }
     default: {  // 3
       ustarb += uob; ptotstarb += ptotob;
-      double db = -O::div(rob * ro, d) - O::div(etotob * etoto, d);
       const double rq = O::div(rob, d);
       rrb += rq * (SR - ur); SRb += rq * rr; urb -= rq * rr;
       const double nEb = O::div(etotob, d);
+      const double db = -(rq * ro + nEb * etoto);
       SRb += nEb * etotr; urb -= nEb * etotr; etotrb += nEb * (SR - ur);
       prb -= nEb * ur; urb -= nEb * pr; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
       SRb += db; ustarb -= db;
@@ -224,10 +224,11 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   double denb = -npb * ptotstar - nub * ustar;
   double rcrb = npb * (pl + rcl * (ul - ur)) + nub * ur + denb;
   double rclb = npb * (pr + rcr * (ul - ur)) + nub * ul + denb;
-  plb += npb * rcr + nub;
-  prb += npb * rcl - nub;
-  ulb += npb * rcl * rcr + nub * rcl;
-  urb += -npb * rcl * rcr + nub * rcr;
+  const double pa = npb * rcr + nub, pb = npb * rcl - nub;
+  plb += pa;
+  prb += pb;
+  ulb += rcl * pa;   // npb rcl rcr + nub rcl
+  urb -= rcr * pb;   // -npb rcl rcr + nub rcr
   // rcr = rr (SR - ur), rcl = rl (ul - SL)
   rrb += rcrb * (SR - ur); SRb += rcrb * rr; urb -= rcrb * rr;
   rlb += rclb * (ul - SL); ulb += rclb * rl; SLb -= rclb * rl;
