@@ -172,9 +172,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(precision: int, nx: int, version: int):
-    """dram bytes (read + write) per launch of the step kernel from the committed
-    ncu summary of the same workload, if there is one."""
+def profiled_value(precision: int, nx: int, version: int, key: str):
+    """A per-launch figure of the step kernel (`dram_bytes_per_launch`,
+    `fp64_warp_inst_per_launch`) from the committed ncu summary of the same
+    workload, if there is one."""
     name = f"k_fused_{nx}_{'fp64' if precision == 8 else 'fp32'}_traffic.txt" if version == 0 else None
     if not name:
         return None
@@ -182,9 +183,13 @@ def profiled_traffic(precision: int, nx: int, version: int):
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             return float(line.split(":")[1])
     return None
+
+
+def profiled_traffic(precision: int, nx: int, version: int):
+    return profiled_value(precision, nx, version, "dram_bytes_per_launch")
 
 
 def workload_name(a):
@@ -470,6 +475,15 @@ def run_ours(a, dist):
         if a.adjoint_batch_steps > 0:
             adjoint_batch = measure_adjoint_batch(E, a)
 
+    fp64_roof = {"pipe": "fp64", "dfma_per_s": dfma, "ddiv_per_s": ddiv,
+                 "note": "the FP64 step is bound by the FP64 pipe (two Riemann solves, traces, slopes per cell), "
+                         "not by HBM"}
+    warp_inst = profiled_value(a.precision, a.nx, a.version, "fp64_warp_inst_per_launch")
+    if warp_inst and a.precision == 8 and a.riemann == "hllc":
+        inst_s = 32 * warp_inst / (kern_ms * 1e-3)  # FP64 thread instructions per second, this run
+        fp64_roof.update({"fp64_inst_per_cell": round(32 * warp_inst / (a.nx * a.nx), 1),
+                          "achieved_per_s": inst_s, "frac": round(inst_s / dfma, 4),
+                          "frac_of": "the live DFMA probe (independent FP64 instructions per second)"})
     if dist.rank == 0:
         isz = a.nx + 4
         line = {
@@ -486,9 +500,7 @@ def run_ours(a, dist):
                          "frac": round(achieved / hbm_peak, 5), "peak_kind": peak_kind,
                          "traffic": traffic,
                          "bytes_per_launch": bytes_per_launch, "kernel_ms": round(kern_ms, 4),
-                         "binding_roof": {"pipe": "fp64", "dfma_per_s": dfma, "ddiv_per_s": ddiv,
-                                          "note": "the FP64 step is bound by the FP64 pipe (divisions and "
-                                                  "square roots of two Riemann solves per cell), not by HBM"}},
+                         "binding_roof": fp64_roof},
             "e2e": e2e,
             "cpu_baseline": cpu,
             "cpu_baseline_multicore": cpu_mc,

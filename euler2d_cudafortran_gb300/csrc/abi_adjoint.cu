@@ -34,7 +34,7 @@ struct e2d_adjoint {
   double* pool = nullptr;  // states: 2 ping-pong + checkpoints + segment
   int nchk = 0, kseg = 0, cap_steps = 0;
   std::vector<StateMap> maps;  // one TMA descriptor per state buffer
-  double* ub[2] = {nullptr, nullptr};
+  double* ub[3] = {nullptr, nullptr, nullptr};  // adjoint states, rotating: read, written, zeroed
   Ctl* ctl = nullptr;
   double* dt_log = nullptr;
   double* inv_log = nullptr;
@@ -173,12 +173,15 @@ void enqueue_recompute(e2d_adjoint* a, int sg, int set, int nsteps, cudaStream_t
 // the second stream into the other set, so the two overlap on the GPU; the
 // last segment needs no recomputation (the forward sweep kept its states).  The
 // running CFL maximum's rises are found on the device from the logged
-// maxima.  Leaves dJ/dU_0 in ub[final_ub(nsteps)].
+// maxima.  The adjoint states rotate over three buffers: reverse step m
+// reads one, accumulates into the next and zeroes the third for step m - 1.
+// Leaves dJ/dU_0 in ub[final_ub(nsteps)].
 void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
   const Hydro<double>& h = a->h;
   cudaStream_t s = a->stream, s2 = a->stream2;
   cudaMemsetAsync(a->dtbar_log, 0, nsteps * sizeof(double), s);
   int cur = 0;  // ub[cur] holds Ubar of the state after the step being reversed
+  cudaMemsetAsync(a->ub[1], 0, a->state_elems * sizeof(double), s);
   const int K = a->kseg, last = (nsteps + K - 1) / K - 1;
   // the last segment's states were kept by the forward sweep
   for (int sg = last; sg >= 0; --sg) {
@@ -190,10 +193,10 @@ void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
       cudaEventRecord(a->join, s2);
     }
     for (int m = k1 - 1; m >= k0; --m) {
-      const int nxt = cur ^ 1;
-      cudaMemsetAsync(a->ub[nxt], 0, a->state_elems * sizeof(double), s);
+      const int nxt = (cur + 1) % 3, zro = (cur + 2) % 3;
       Field<double> um = state(a, seg_index(a, set, m - k0));
-      launch_step_rev(h, um, ubf(a, cur), ubf(a, nxt), a->dt_log + m, a->dtbar_log + m, s);
+      launch_step_rev(h, um, ubf(a, cur), ubf(a, nxt), m > 0 ? ubf(a, zro) : Field<double>{nullptr, 0, 0},
+                      a->dt_log + m, a->dtbar_log + m, s);
       if (dt_mode == 1) {
         launch_argmax(h, um, a->part_v, a->part_i, a->nparts, a->inv_log, m, s);
         launch_dt_route(h, um, ubf(a, nxt), a->part_v, a->part_i, a->nparts, a->dtbar_log, a->inv_log, m, nsteps,
@@ -205,7 +208,7 @@ void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
   }
 }
 
-int final_ub(int nsteps) { return nsteps & 1; }  // one ub swap per reversed step
+int final_ub(int nsteps) { return nsteps % 3; }  // one rotation per reversed step
 
 int check_health(e2d_adjoint* a) {
   unsigned health = 0;
@@ -254,6 +257,7 @@ int e2d_adjoint_create(const e2d_params* p, e2d_adjoint** out) {
   a->nparts = std::min(1024, p->ny);
   const size_t sb = a->state_elems * sizeof(double);
   if (cudaMalloc(&a->ub[0], sb) != cudaSuccess || cudaMalloc(&a->ub[1], sb) != cudaSuccess ||
+      cudaMalloc(&a->ub[2], sb) != cudaSuccess ||
       cudaMalloc(&a->ctl, sizeof(Ctl)) != cudaSuccess || cudaMalloc(&a->J, sizeof(double)) != cudaSuccess ||
       cudaMalloc(&a->part_v, a->nparts * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&a->part_i, a->nparts * sizeof(long long)) != cudaSuccess) {
@@ -280,6 +284,7 @@ int e2d_adjoint_destroy(e2d_adjoint* a) {
   free_buffers(a);
   cudaFree(a->ub[0]);
   cudaFree(a->ub[1]);
+  cudaFree(a->ub[2]);
   cudaFree(a->ctl);
   cudaFree(a->J);
   cudaFree(a->part_v);

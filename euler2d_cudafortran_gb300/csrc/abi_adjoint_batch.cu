@@ -13,7 +13,8 @@
 // (indices into its slab): 0, 1 forward ping-pong; 2.. checkpoints every
 // K = ceil(sqrt(N)) steps; then two sets of K segment states (a segment is
 // reversed on the main stream from one set while the next is recomputed on a
-// second stream into the other); then 2 adjoint states.  The initial state
+// second stream into the other); then 3 adjoint states (rotating: read,
+// accumulated into, zeroed for the next reverse step).  The initial state
 // lives in its own array so that a call can be replayed.
 #include <cuda_runtime.h>
 
@@ -72,7 +73,7 @@ int abfail(int code, const std::string& m) { return set_error(code, m); }
 constexpr int kPing = 0, kChk = 2;
 int seg_base(const e2d_adjoint_batch* b) { return kChk + b->nchk; }
 int ub_base(const e2d_adjoint_batch* b) { return kChk + b->nchk + 2 * b->kseg; }
-int nbuf(const e2d_adjoint_batch* b) { return ub_base(b) + 2; }
+int nbuf(const e2d_adjoint_batch* b) { return ub_base(b) + 3; }
 
 void clear_graphs(e2d_adjoint_batch* b) {
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
@@ -274,13 +275,14 @@ void enqueue_recompute(e2d_adjoint_batch* b, int sg, int set, int nsteps, cudaSt
 
 // Reverse sweep, segment sg from set sg & 1 on the main stream while segment
 // sg - 1 is recomputed into the other set on the second stream; dJ/dU_0 ends
-// in buffer ub_base + (nsteps & 1).
+// in buffer ub_base + (nsteps % 3).
 void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
   cudaStream_t s = b->stream, s2 = b->stream2;
   const AdjBatch B = view(b);
   cudaMemsetAsync(b->dtbar_log, 0, sizeof(double) * nsteps * b->nprob, s);
   const int K = b->kseg, ub = ub_base(b), last = (nsteps + K - 1) / K - 1;
   int cur = 0;
+  launch_batch_copy(B, ub + 1, ub + 1, s);  // zero
   // the last segment's states were kept by the forward sweep
   for (int sg = last; sg >= 0; --sg) {
     const int set = sg & 1, k0 = sg * K, k1 = std::min(k0 + K, nsteps), sb = seg_base(b) + set * K;
@@ -291,9 +293,8 @@ void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
       cudaEventRecord(b->join, s2);
     }
     for (int m = k1 - 1; m >= k0; --m) {
-      const int nxt = cur ^ 1;
-      launch_batch_copy(B, ub + nxt, ub + nxt, s);  // zero
-      launch_batch_step_rev(B, sb + (m - k0), ub + cur, ub + nxt, m, s);
+      const int nxt = (cur + 1) % 3, zro = (cur + 2) % 3;
+      launch_batch_step_rev(B, sb + (m - k0), ub + cur, ub + nxt, m > 0 ? ub + zro : -1, m, s);
       if (dt_mode == 1) {
         launch_batch_argmax(B, sb + (m - k0), m, s);
         launch_batch_dt_route(B, sb + (m - k0), ub + nxt, m, nsteps, s);

@@ -32,7 +32,7 @@ struct AdjBatch {
 
 int batch_step_rev_setup();
 int rev_tile_shape(int* tx, int* ty);
-void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int m, cudaStream_t s);
+void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s);
 void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s);
 void launch_batch_dt_route(const AdjBatch& B, int un, int ub_out, int m, int nsteps, cudaStream_t s);
 // J[p] += sum rho^2 w of buffer un; seed_ub >= 0: that buffer = dJ/dU on the interior.
@@ -46,9 +46,10 @@ void launch_batch_extract(const AdjBatch& B, int ub, double* out, cudaStream_t s
 size_t step_rev_smem();
 int step_rev_setup();
 // Ubar_n += reverse of one step (U_n with ghosts, Ubar_{n+1} interior); *dtbar += dJ/d dt.
-// dt is read on the device (the logged dt of the step).
+// dt is read on the device (the logged dt of the step).  The interior of ubz
+// (if ubz.p) is zeroed: the buffer the following reverse step accumulates into.
 void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn1, Field<double> ubn,
-                     const double* dt, double* dtbar, cudaStream_t s);
+                     Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s);
 // Ghost corners of segment buffers seg_index + 1 .. seg_index + nseg - 1 (states k0 + j)
 // from ping-pong buffer ping_index + ((k0 + j) & 1); buffers are state_elems apart in pool.
 void launch_seg_corners(const Hydro<double>& h, double* pool, size_t state_elems, size_t pitch, size_t plane,

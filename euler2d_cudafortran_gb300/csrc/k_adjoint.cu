@@ -43,9 +43,11 @@ constexpr int N_SMEM = QB_OFF + 4 * NBOX;
 constexpr size_t SMEM_BYTES = (size_t)N_SMEM * sizeof(double) + 64;
 
 // One 32 x 7 tile (bx, by) of the reverse step; sm is the dynamic shared area.
+// ubz (if set) is the adjoint buffer of the following reverse step: the
+// tile's interior cells of it are zeroed here (nothing reads it now).
 __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
-                                              Field<double> ubn, double dt, double* dtbar, int bx, int by,
-                                              double* sm) {
+                                              Field<double> ubn, Field<double> ubz, double dt, double* dtbar,
+                                              int bx, int by, double* sm) {
   double* sq = sm + Q_OFF;
   double* sdq = sm + DQ_OFF;
   double* ss = sm + S_OFF;
@@ -56,6 +58,12 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   const int tid = threadIdx.x;
   const int i0 = GW + bx * ATX, j0 = GW + by * ATY;
   const double dtdx = dt / h.dx, dtdy = dt / h.dy;
+  if (ubz.p) {
+    for (int k = tid; k < 4 * ATX * ATY; k += ANT) {
+      const int v = k / (ATX * ATY), rem = k - v * (ATX * ATY), y = rem / ATX, x = rem - y * ATX;
+      if (i0 + x <= h.nx + 1 && j0 + y <= h.ny + 1) ubz.at(v, j0 + y, i0 + x) = 0.0;
+    }
+  }
 
   // ---- load U box, Ubar' of cells [i0-1, i0+ATX) x [j0-1, j0+ATY), zero accumulators
   for (int k = tid; k < 4 * NBOX; k += ANT) {
@@ -307,10 +315,10 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
 }
 
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
-    k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, const double* dt,
-               double* dtbar) {
+    k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, Field<double> ubz,
+               const double* dt, double* dtbar) {
   extern __shared__ double sm[];
-  step_rev_tile(h, un, ubn1, ubn, *dt, dtbar, blockIdx.x, blockIdx.y, sm);
+  step_rev_tile(h, un, ubn1, ubn, ubz, *dt, dtbar, blockIdx.x, blockIdx.y, sm);
 }
 
 // The 2x2 ghost corners are never written by a step, so a state keeps the
@@ -378,26 +386,42 @@ __device__ __forceinline__ void argmax_part(const Hydro<double>& h, Field<double
 // If the running maximum rises at state m, the steps [m, n1) up to the next
 // rise use the compute_dt term of the argmax cell of state m; their dt
 // adjoints go to Ubar_m: dt_n = cfl / inv_n, d dt_n / d inv_n = -cfl / inv_n^2.
-// One thread; logs have stride `stride`.
+// One warp (called by all 32 lanes); logs have stride `stride`.
 __device__ __forceinline__ void dt_route(const Hydro<double>& h, Field<double> u, Field<double> ub, const double* pv,
                                          const long long* pi, int nparts, const double* dtbar_log,
                                          const double* inv_log, int stride, int m, int nsteps) {
-  int n1 = m + 1;
-  while (n1 < nsteps && !max_rises(inv_log, n1, stride)) ++n1;
+  const int lane = threadIdx.x & 31;
+  // the argmax over the partial results (largest term, lowest index on ties)
   double best = -1.0;
   long long bi = 0x7fffffffffffffffll;
-  for (int k = 0; k < nparts; ++k)
+  for (int k = lane; k < nparts; k += 32)
     if (pv[k] > best || (pv[k] == best && pi[k] < bi)) { best = pv[k]; bi = pi[k]; }
-  double s = 0.0;
-  for (int n = m; n < n1; ++n) {
-    const double inv = inv_log[(long long)n * stride];
-    s += -h.cfl / (inv * inv) * dtbar_log[(long long)n * stride];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(0xffffffffu, best, o);
+    const long long i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (v2 > best || (v2 == best && i2 < bi)) { best = v2; bi = i2; }
   }
+  // n1: the next state after m where the maximum rises (or nsteps)
+  int n1 = nsteps;
+  for (int base = m + 1; base < nsteps; base += 32) {
+    const int n = base + lane;
+    const unsigned rise = __ballot_sync(0xffffffffu, n < nsteps && max_rises(inv_log, n, stride));
+    if (rise) { n1 = base + __ffs(rise) - 1; break; }
+  }
+  double sacc = 0.0;
+  for (int n = m + lane; n < n1; n += 32) {
+    const double inv = inv_log[(long long)n * stride];
+    sacc += -h.cfl / (inv * inv) * dtbar_log[(long long)n * stride];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+  if (lane != 0) return;
   const int j = (int)(bi / h.isize), i = (int)(bi - (long long)j * h.isize);
   double uc[4], g[4] = {0, 0, 0, 0};
 #pragma unroll
   for (int v = 0; v < 4; ++v) uc[v] = u.at(v, j, i);
-  adj::cell_invdt_rev(h, uc, s, g);
+  adj::cell_invdt_rev(h, uc, sacc, g);
 #pragma unroll
   for (int v = 0; v < 4; ++v) ub.at(v, j, i) += g[v];
 }
@@ -411,7 +435,7 @@ __global__ void k_argmax_partial(Hydro<double> h, Field<double> u, double* pv, l
 __global__ void k_dt_route(Hydro<double> h, Field<double> u, Field<double> ub, const double* pv,
                            const long long* pi, int nparts, const double* dtbar_log, const double* inv_log, int m,
                            int nsteps) {
-  if (threadIdx.x != 0 || blockIdx.x != 0 || !max_rises(inv_log, m, 1)) return;
+  if (!max_rises(inv_log, m, 1)) return;  // uniform over the warp
   dt_route(h, u, ub, pv, pi, nparts, dtbar_log, inv_log, 1, m, nsteps);
 }
 
@@ -463,7 +487,7 @@ __device__ __forceinline__ Field<double> afield(const AdjProb& P, int k) {
 // tile list (problem p owns tiles [tile_begin, tile_begin + ntx * nty)).
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_batch_step_rev(const AdjProb* __restrict__ probs, int nprob, const double* dt_log, double* dtbar_log, int un,
-                     int ub_in, int ub_out, int m) {
+                     int ub_in, int ub_out, int ub_zero, int m) {
   extern __shared__ double sm[];
   __shared__ Hydro<double> sh;
   __shared__ int sp;
@@ -482,7 +506,8 @@ __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
   const AdjProb& P = probs[sp];
   const int tile = t - P.tile_begin;
   const long long row = (long long)m * nprob + sp;
-  step_rev_tile(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out), dt_log[row], dtbar_log + row,
+  step_rev_tile(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out),
+                ub_zero >= 0 ? afield(P, ub_zero) : Field<double>{nullptr, 0, 0}, dt_log[row], dtbar_log + row,
                 tile % P.ntx, tile / P.ntx, sm);
 }
 
@@ -499,7 +524,7 @@ __global__ void k_batch_dt_route(const AdjProb* __restrict__ probs, int nprob, c
                                  int nparts, const double* dtbar_log, const double* inv_log, int un, int ub_out,
                                  int m, int nsteps) {
   const int p = blockIdx.x;
-  if (threadIdx.x != 0 || !max_rises(inv_log + p, m, nprob)) return;
+  if (!max_rises(inv_log + p, m, nprob)) return;  // uniform over the warp
   const AdjProb& P = probs[p];
   dt_route(P.h, afield(P, un), afield(P, ub_out), pv + (long long)p * nparts, pi + (long long)p * nparts, nparts,
            dtbar_log + p, inv_log + p, nprob, m, nsteps);
@@ -557,9 +582,9 @@ int step_rev_setup() {
 }
 
 void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn1, Field<double> ubn,
-                     const double* dt, double* dtbar, cudaStream_t s) {
+                     Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s) {
   dim3 g((h.nx + ATX - 1) / ATX, (h.ny + ATY - 1) / ATY);
-  k_step_rev<<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, dt, dtbar);
+  k_step_rev<<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar);
 }
 
 void launch_seg_corners(const Hydro<double>& h, double* pool, size_t state_elems, size_t pitch, size_t plane,
@@ -598,9 +623,9 @@ int rev_tile_shape(int* tx, int* ty) {
   return 0;
 }
 
-void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int m, cudaStream_t s) {
+void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s) {
   k_batch_step_rev<<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in, ub_out,
-                                                          m);
+                                                          ub_zero, m);
 }
 
 void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s) {
