@@ -215,3 +215,36 @@ def test_health_flags_negative_density(e2d):
         run.set_state(0, u)
         run.advance(0, 1)
         assert run.health() & e2d.HEALTH_NEG_DENSITY
+
+
+SCHEMES = [
+    dict(slope_type=0, riemann=2),                          # first order (zero slopes)
+    dict(slope_type=0, riemann=0),
+    dict(slope_type=1, riemann=0),                          # minmod
+    dict(niter_riemann=0, riemann=0),                       # two-shock solver without Newton iterations
+    dict(niter_riemann=1, riemann=0),
+    dict(gamma0=5.0 / 3.0, cfl=0.5, riemann=2),
+    dict(gamma0=5.0 / 3.0, cfl=0.5, riemann=0),
+    dict(smallr=1e-3, smallc=1e-2, riemann=2),              # floors that bite in the low state
+    dict(smallr=1e-3, smallc=1e-2, riemann=0),
+]
+
+
+@pytest.mark.parametrize("scheme", SCHEMES, ids=lambda d: "-".join(f"{k}{v:.4g}" if isinstance(v, float) else
+                                                                  f"{k}{v}" for k, v in d.items()))
+@pytest.mark.parametrize("version", [0, 1, 2])
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+def test_scheme_parameters_bitwise(e2d, oracle, scheme, version, prec):
+    """Every &HYDRO parameter the step reads: slope_type, niter_riemann,
+    gamma0, cfl, smallr, smallc, with both Riemann solvers."""
+    kw = dict(scheme)
+    riemann = kw.pop("riemann")
+    nx, ny, n = 64, 48, 20
+    pe = e2d.make_params(nx=nx, ny=ny, implementation_version=version, riemann_solver=riemann, precision=prec,
+                         boundary_type_xmin=1, boundary_type_xmax=2, boundary_type_ymin=3, boundary_type_ymax=3,
+                         **{"gamma0": 1.4, "cfl": 0.8, **kw})
+    po = oracle.Params(nx=nx, ny=ny, riemann=riemann, bc_xmin=1, bc_xmax=2, bc_ymin=3, bc_ymax=3,
+                       **{"gamma0": 1.4, "cfl": 0.8, **kw})
+    ref, dts_ref, _, _ = oracle.run(po, n, prec="f64" if prec == 8 else "f32", nthreads=NTHREADS)
+    gpu, dts = e2d.run_steps(n, pe)
+    assert_same(gpu, ref, dts, dts_ref, f"{scheme} v{version} prec={prec}")
