@@ -43,7 +43,6 @@ void launch_batch_copy(const AdjBatch& B, int src, int dst, cudaStream_t s);
 void launch_batch_seg_corners(const AdjBatch& B, int ping, int seg, int k0, int nseg, cudaStream_t s);
 void launch_batch_extract(const AdjBatch& B, int ub, double* out, cudaStream_t s);
 
-size_t step_rev_smem();
 int step_rev_setup();
 // Ubar_n += reverse of one step (U_n with ghosts, Ubar_{n+1} interior); *dtbar += dJ/d dt.
 // dt is read on the device (the logged dt of the step).  The interior of ubz

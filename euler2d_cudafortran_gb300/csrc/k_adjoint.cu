@@ -572,8 +572,6 @@ __global__ void k_batch_extract(const AdjProb* __restrict__ probs, int ub, doubl
 
 }  // namespace
 
-size_t step_rev_smem() { return SMEM_BYTES; }
-
 int step_rev_setup() {
   return cudaFuncSetAttribute(k_step_rev, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
                  cudaSuccess

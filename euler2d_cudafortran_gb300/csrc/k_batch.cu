@@ -86,6 +86,8 @@ struct Variant {
     int n = 0;
     if (cudaFuncSetAttribute(k_batch_step<Real, C, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)C::bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(k_batch_step<Real, C, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<Real, C, MINB>, C::NT, C::bytes) !=
             cudaSuccess) {
       cudaGetLastError();
@@ -100,7 +102,7 @@ struct Variant {
 };
 
 // Tile shapes offered to the autotuner.
-template <typename Real> using V32x15 = Variant<Real, TileCfg<Real, 32, 15, 256>, (sizeof(Real) == 8 ? 2 : 3)>;
+template <typename Real> using V32x15 = Variant<Real, TileCfg<Real, 32, 15, 256>, (sizeof(Real) == 8 ? 2 : 4)>;
 template <typename Real> using V32x7 = Variant<Real, TileCfg<Real, 32, 7, 128>, (sizeof(Real) == 8 ? 4 : 6)>;
 
 }  // namespace

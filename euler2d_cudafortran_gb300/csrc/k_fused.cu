@@ -27,7 +27,8 @@ struct FusedPlan {
 namespace {
 
 // Tile of the single-run kernel: 32 x 15 cells, 256 threads; 2 CTAs per SM
-// in FP64 (register bound), 3 in FP32.
+// in FP64 (register bound), 4 in FP32 (64 registers; 4 x 55 KB of shared
+// memory, which needs the largest shared-memory carveout).
 template <typename Real> struct FusedTile { using C = TileCfg<Real, 32, 15, 256>; };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -51,7 +52,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? 2 : 3)
+__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? 2 : 4)
     k_fused(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
             StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
   using C = typename FusedTile<Real>::C;
@@ -117,6 +118,17 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Dynamic shared memory of the tile, and the largest shared-memory carveout
+// so that as many CTAs as the launch bounds ask for fit on an SM.
+template <typename Real>
+bool set_fused_attributes() {
+  using C = typename FusedTile<Real>::C;
+  return cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
+}
+
 EncodeTiledFn get_encode_fn() {
   static EncodeTiledFn fn = nullptr;
   if (!fn) {
@@ -158,8 +170,8 @@ FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2
     delete p;
     return nullptr;
   }
-  if (cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) !=
-      cudaSuccess) {
+  if (!set_fused_attributes<Real>()) {
+    cudaGetLastError();
     delete p;
     return nullptr;
   }
@@ -180,8 +192,10 @@ template <typename Real>
 bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out) {
   static_assert(sizeof(StateMap) == sizeof(CUtensorMap), "descriptor size");
   using C = typename FusedTile<Real>::C;
-  if (cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess)
+  if (!set_fused_attributes<Real>()) {
+    cudaGetLastError();
     return false;
+  }
   return encode_state_map<Real>(reinterpret_cast<CUtensorMap*>(out->bytes), h, u);
 }
 
