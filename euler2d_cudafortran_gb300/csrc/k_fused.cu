@@ -26,10 +26,19 @@ struct FusedPlan {
 
 namespace {
 
-// Tile of the single-run kernel: 32 x 15 cells, 256 threads; 2 CTAs per SM
-// in FP64 (register bound), 4 in FP32 (64 registers; 4 x 55 KB of shared
-// memory, which needs the largest shared-memory carveout).
-template <typename Real> struct FusedTile { using C = TileCfg<Real, 32, 15, 256>; };
+// Tile of the single-run kernel, 256 threads.  FP64: 32 x E2D_FUSED_TY64
+// cells at E2D_FUSED_MINB64 CTAs per SM (shared memory and registers must
+// allow that many); FP32: 32 x 15 cells at 4 CTAs per SM (64 registers, 4 x
+// 55 KB of shared memory).  Both need the largest shared-memory carveout.
+#ifndef E2D_FUSED_TY64
+#define E2D_FUSED_TY64 15
+#endif
+#ifndef E2D_FUSED_MINB64
+#define E2D_FUSED_MINB64 2
+#endif
+template <typename Real> struct FusedTile;
+template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, 256>; };
+template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -52,7 +61,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? 2 : 4)
+__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
             StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
   using C = typename FusedTile<Real>::C;
