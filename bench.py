@@ -453,7 +453,8 @@ def run_ours(a, dist):
     variants = None
     if dist.rank == 0 and not a.no_variants:
         variants = []
-        for (nx, prec, ver) in ((2048, 8, 1), (2048, 4, 0), (2048, 4, 1), (4096, 8, 0), (4096, 4, 0)):
+        for (nx, prec, ver) in ((2048, 8, 1), (2048, 4, 0), (2048, 4, 1), (4096, 8, 0), (4096, 8, 1), (4096, 4, 0),
+                                (4096, 4, 1)):
             p = E.make_params(nx=nx, ny=nx, gamma0=1.4, cfl=0.8, implementation_version=ver,
                               riemann_solver=params.riemann_solver, precision=prec)
             with E.HydroRun(p) as r3:
@@ -465,6 +466,24 @@ def run_ours(a, dist):
                 vms = r3.last_advance_ms()
             variants.append({"nx": nx, "precision": "FP64" if prec == 8 else "FP32", "implementationVersion": ver,
                              "steps": ns, "mcells_per_s": round(nx * nx * ns / (vms * 1e-3) / 1e6, 2)})
+
+    # FP32 against the FP64 oracle: the FP64 run is bitwise the oracle's, so
+    # its state after `steps` steps stands for it
+    fp32_error = None
+    if dist.rank == 0 and not a.no_variants:
+        finals = {}
+        for prec in (8, 4):
+            p = E.make_params(nx=a.nx, ny=a.nx, gamma0=1.4, cfl=0.8, implementation_version=0,
+                              riemann_solver=params.riemann_solver, precision=prec)
+            with E.HydroRun(p) as r4:
+                r4.init_implode()
+                dts4 = r4.advance(0, a.steps)
+                finals[prec] = (r4.final_state(a.steps)[:, 2:-2, 2:-2].astype(np.float64), dts4.astype(np.float64))
+        (u64, dt64), (u32, dt32) = finals[8], finals[4]
+        rel = [float(np.abs(u32[v] - u64[v]).sum() / np.abs(u64[v]).sum()) for v in range(4)]
+        fp32_error = {"workload": f"{a.nx}x{a.nx}, {a.steps} steps, implementationVersion 0",
+                      "rel_l1_per_variable": {"rho": rel[0], "E": rel[1], "rho_u": rel[2], "rho_v": rel[3]},
+                      "dt_max_rel": float(np.max(np.abs(dt32 - dt64) / dt64))}
 
     batched = None
     if dist.rank == 0 and not a.no_batched:
@@ -508,6 +527,7 @@ def run_ours(a, dist):
             "gpu_launches": a.steps + 1 if a.version == 0 else 4 * a.steps,
             "health_flags": health,
             "variants": variants,
+            "fp32_error_vs_fp64_oracle": fp32_error,
             "batched": batched,
             "adjoint": adjoint,
             "adjoint_batched": adjoint_batch,
