@@ -48,7 +48,8 @@ EXPORTED_SYMBOLS = [
     "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
     "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
-    "e2d_godunov_unsplit_noalloc", "e2d_selftest_arith", "e2d_begin_download", "e2d_wait_download",
+    "e2d_godunov_unsplit_noalloc", "e2d_selftest_arith", "e2d_selftest_wait", "e2d_begin_download",
+    "e2d_wait_download",
     "e2d_host_alloc", "e2d_host_free",
     "e2d_batch_create", "e2d_batch_destroy", "e2d_batch_init_diagonal", "e2d_batch_upload_state",
     "e2d_batch_download_state", "e2d_batch_advance", "e2d_batch_last_advance_ms", "e2d_batch_set_schedule",
@@ -117,6 +118,7 @@ def load_library(path: str = LIB_PATH):
         "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
                              ctypes.POINTER(ctypes.c_size_t)],
         "e2d_godunov_unsplit_noalloc": [ctypes.POINTER(Params), vp, vp, ctypes.c_size_t, d, vp],
+        "e2d_selftest_wait": [ctypes.c_longlong, ip, ip, ctypes.POINTER(ctypes.c_longlong)],
         "e2d_begin_download": [vp, i, vp],
         "e2d_wait_download": [vp],
         "e2d_host_alloc": [ctypes.c_size_t, ctypes.POINTER(vp)],
@@ -551,6 +553,13 @@ def measure_fp64_peak():
     a, b = ctypes.c_double(), ctypes.c_double()
     _check(load_library().e2d_measure_fp64_peak(ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+def selftest_wait(limit_cycles: int = 1 << 24):
+    """(arrived barrier completed, silent barrier completed, cycles waited on the silent one)."""
+    a, b, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+    _check(load_library().e2d_selftest_wait(limit_cycles, ctypes.byref(a), ctypes.byref(b), ctypes.byref(w)))
+    return bool(a.value), bool(b.value), w.value
 
 
 def selftest_arith(op: int, mode: int, n: int, seed: int = 1, rates: bool = False):

@@ -16,6 +16,7 @@
 //      next step's CFL maximum (block max + atomic max into a run slot).
 // Primitives, slopes, face states and fluxes never leave shared memory.
 #include <cuda.h>
+#include "sync.cuh"
 #include "tile.cuh"
 
 namespace e2d {
@@ -39,26 +40,6 @@ namespace {
 template <typename Real> struct FusedTile;
 template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, 256>; };
 template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Bounded wait on an mbarrier phase: gives up after ~2^31 SM cycles (about a
-// second) and reports false, so a lost transfer cannot hang the GPU.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (true) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (clock64() - t0 > (1ll << 31)) return false;
-  }
-}
 
 template <typename Real>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
@@ -102,7 +83,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
         : "memory");
   }
   const Real dt = sdt[0];
-  const bool ok = mbar_wait(bar_a, 0);
+  const bool ok = mbar_wait(bar_a, 0, kTmaWaitCycles);
   if (__syncthreads_or(!ok)) {
     if (tid == 0) atomicOr(&ctl->health, 4u);
     return;

@@ -6,6 +6,7 @@
 
 #include "../../include/euler2d_gb300.h"
 #include "emul64.cuh"
+#include "sync.cuh"
 
 namespace {
 
@@ -90,7 +91,47 @@ __global__ void k_rate(int op, int emulated, int iters, double* out) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
 }
 
+// The bounded mbarrier wait of the step kernels, exercised without any copy
+// in flight: barrier A receives its single arrival and must complete at once;
+// barrier B is never arrived on (a flag nothing sets) and the wait must give
+// up after limit_cycles.  out[0] = A completed, out[1] = B completed,
+// out[2] = cycles spent waiting on B.
+__global__ void k_wait_probe(long long limit_cycles, long long* out) {
+  __shared__ __align__(8) uint64_t bars[2];
+  if (threadIdx.x != 0) return;
+  const uint32_t a = e2d::smem_u32(&bars[0]), b = e2d::smem_u32(&bars[1]);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+  out[0] = e2d::mbar_wait(a, 0, limit_cycles) ? 1 : 0;
+  const long long t0 = clock64();
+  out[1] = e2d::mbar_wait(b, 0, limit_cycles) ? 1 : 0;
+  out[2] = clock64() - t0;
+}
+
 }  // namespace
+
+extern "C" int e2d_selftest_wait(long long limit_cycles, int* arrived_completed, int* silent_completed,
+                                 long long* waited_cycles) {
+  if (limit_cycles < 1 || limit_cycles > (1ll << 32) || !arrived_completed || !silent_completed)
+    return E2D_ERR_INVALID_ARG;
+  long long* d = nullptr;
+  if (cudaMalloc(&d, 3 * sizeof(long long)) != cudaSuccess) {
+    cudaGetLastError();
+    return E2D_ERR_NO_DEVICE;
+  }
+  long long h[3] = {0, 0, 0};
+  k_wait_probe<<<1, 32>>>(limit_cycles, d);
+  const bool ok = cudaGetLastError() == cudaSuccess &&
+                  cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(d);
+  if (!ok) return E2D_ERR_CUDA;
+  *arrived_completed = (int)h[0];
+  *silent_completed = (int)h[1];
+  if (waited_cycles) *waited_cycles = h[2];
+  return E2D_OK;
+}
 
 extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* first_bad, double* emulated_per_s,

@@ -144,6 +144,16 @@ int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
 int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed, unsigned long long* mismatches,
                        double* first_bad, double* emulated_per_s, double* native_per_s);
 
+/* Self-test of the bounded wait every kernel wait goes through (the step
+ * kernels' TMA wait gives up after about a second and raises health flag 4):
+ * one mbarrier that receives its arrival must complete (*arrived_completed =
+ * 1), one that nothing arrives on must give up after limit_cycles SM cycles
+ * (*silent_completed = 0, *waited_cycles about limit_cycles), with no copy in
+ * flight and the context usable afterwards.  Not part of the reference; used
+ * by the tests of failure detection. */
+int e2d_selftest_wait(long long limit_cycles, int* arrived_completed, int* silent_completed,
+                      long long* waited_cycles);
+
 /* Current running maximum of 1/dt (double, whatever the precision). */
 int e2d_get_invdt(e2d_run* h, double* invdt);
 

@@ -114,3 +114,18 @@ def test_adjoint_create_rejects_invalid_arguments(e2d):
     assert lib.e2d_adjoint_batch_destroy(None) == e2d.E2D_OK
     J = ctypes.c_double()
     assert lib.e2d_adjoint_batch_objective(None, 10, 0.6, 0.6, 0.1, ctypes.byref(J)) == e2d.E2D_ERR_INVALID_ARG
+
+
+def test_async_download_and_selftest_reject_invalid_arguments(e2d):
+    lib = e2d.load_library()
+    buf = ctypes.create_string_buffer(64)
+    assert lib.e2d_begin_download(None, 0, buf) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_wait_download(None) == e2d.E2D_ERR_INVALID_ARG
+    p = ctypes.c_void_p()
+    assert lib.e2d_host_alloc(0, ctypes.byref(p)) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_host_alloc(64, None) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_host_free(None) == e2d.E2D_OK
+    a, b = ctypes.c_int(), ctypes.c_int()
+    assert lib.e2d_selftest_wait(0, ctypes.byref(a), ctypes.byref(b), None) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_selftest_wait(1 << 40, ctypes.byref(a), ctypes.byref(b), None) == e2d.E2D_ERR_INVALID_ARG
+    assert lib.e2d_selftest_wait(1000, None, ctypes.byref(b), None) == e2d.E2D_ERR_INVALID_ARG

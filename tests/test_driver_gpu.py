@@ -1,4 +1,5 @@
-"""The C++ HydroRun driver end to end, and the asynchronous output path.
+"""The C++ HydroRun driver end to end (the device-resident loop and the
+reference's per-call loop), and the asynchronous output path.
 
 The driver's default output is asynchronous (device snapshot in stream
 order, copy on a second stream, VTK file written by a worker thread while
@@ -67,8 +68,11 @@ def test_async_and_sync_output_identical(e2d, oracle, tmp_path):
     a = run_driver(build.EXE, str(nml), str(tmp_path / "async"))
     s = run_driver(build.EXE, str(nml), str(tmp_path / "sync"), "--sync-io")
     assert a == s and len(a) == 6  # steps 0, 5, 10, 15, 20 and the final 23
+    c = run_driver(build.EXE, str(nml), str(tmp_path / "percall"), "--percall")
+    assert c == a
     for name in a:
         assert (tmp_path / "async" / name).read_bytes() == (tmp_path / "sync" / name).read_bytes(), name
+        assert (tmp_path / "percall" / name).read_bytes() == (tmp_path / "sync" / name).read_bytes(), name
     # serial_ref/main.f90:81 writes u at the end: after 23 steps that is u after step 22
     po = oracle.Params(nx=48, ny=40, gamma0=1.4, cfl=0.8, riemann=0, bc_xmin=1, bc_xmax=2, bc_ymin=1, bc_ymax=3)
     _, _, u, _ = oracle.run(po, 23)
