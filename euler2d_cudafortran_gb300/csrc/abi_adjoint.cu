@@ -3,11 +3,13 @@
 // respect to the initial density field.
 //
 // Forward: the N steps of the run (device-resident dt, as e2d_advance), with
-// a checkpoint of the state every K = ceil(sqrt(N)) steps and logs of dt_n and
-// of the running CFL maximum inv_n.  Reverse: for each segment, last first,
-// the states of the segment are recomputed from its checkpoint with the logged
-// dt (bit for bit the forward states), then the reverse step kernel runs from
-// the last state of the segment back to its first.  dt_mode 0 keeps every dt
+// a checkpoint of the state every K = ceil(sqrt(N)) steps, the states of the
+// last segment kept whole, and logs of dt_n and of the running CFL maximum
+// inv_n.  Reverse: for each segment, last first, the reverse step kernel runs
+// from the last state of the segment back to its first, while the previous
+// segment's states are recomputed from its checkpoint with the logged dt (bit
+// for bit the forward states) on a second stream into a second set of
+// segment buffers.  The whole gradient is one captured graph.  dt_mode 0 keeps every dt
 // frozen; dt_mode 1 also differentiates dt_n = cfl / inv_n through the
 // running maximum: the adjoint of inv_n goes to the cell whose compute_dt
 // term set that maximum, in the state where it was first reached.
@@ -31,7 +33,7 @@ struct e2d_adjoint {
   Hydro<double> h;
   int device = 0;
   size_t pitch = 0, plane = 0, state_elems = 0;
-  double* pool = nullptr;  // states: 2 ping-pong + checkpoints + segment
+  double* pool = nullptr;  // states: 2 ping-pong, the checkpoints, 2 sets of K segment states
   int nchk = 0, kseg = 0, cap_steps = 0;
   std::vector<StateMap> maps;  // one TMA descriptor per state buffer
   double* ub[3] = {nullptr, nullptr, nullptr};  // adjoint states, rotating: read, written, zeroed
