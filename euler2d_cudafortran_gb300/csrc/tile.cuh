@@ -83,8 +83,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
 
   // ---- slopes and trace source terms of the ring cells (-1..TX, -1..TY)
   auto Q = [&](int v, int y, int x) -> Real { return sq[(v * BYs + y) * BXs + x]; };
+  // ring cells in warp-aligned rows: the first TX columns of every row, then
+  // the last RX - TX columns (a warp then reads one row of consecutive words)
+  static_assert(RX - TX == 2, "the ring is two columns wider than the tile");
   for (int k = tid; k < RX * RY; k += NT) {
-    const int x = k % RX + 1, y = k / RX + 1;  // box coordinates
+    const int x = k < TX * RY ? k % TX + 1 : TX + 1 + (k - TX * RY) % 2;  // box coordinates
+    const int y = k < TX * RY ? k / TX + 1 : (k - TX * RY) / 2 + 1;
+    const int kr = (y - 1) * RX + (x - 1);                                 // ring index
     Real qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -95,9 +100,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     trace_sources(h, qc, dqx, dqy, s);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      sdq[v * RX * RY + k] = dqx[v];
-      sdq[(4 + v) * RX * RY + k] = dqy[v];
-      ss[v * RX * RY + k] = s[v];
+      sdq[v * RX * RY + kr] = dqx[v];
+      sdq[(4 + v) * RX * RY + kr] = dqy[v];
+      ss[v * RX * RY + kr] = s[v];
     }
   }
   __syncthreads();
@@ -112,7 +117,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     if (chunk >= NF) break;
     const int k = chunk + lane;
     if (k < NXF) {
-      const int f = k % (TX + 1), r = k / (TX + 1);  // between ring cells (f-1, r) and (f, r)
+      // x faces: the first TX of every row as warp-aligned blocks of TX (a
+      // warp reads one row of consecutive words: no shared-memory bank
+      // conflicts), then the last column, one face per row
+      const int f = k < TX * TY ? k % TX : TX, r = k < TX * TY ? k / TX : k - TX * TY;  // between ring cells (f-1, r) and (f, r)
       if (i0 + f <= h.nx + 2 && j0 + r <= h.ny + 1) {
         const int kl = (r + 1) * RX + f, kr = kl + 1;
         Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
