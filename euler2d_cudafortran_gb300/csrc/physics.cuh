@@ -327,7 +327,7 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   flux[ID] = ro * uo;
   flux[IU] = ((ro * uo) * uo) + ptoto;
   flux[IP] = (etoto + ptoto) * uo;
-  flux[IV] = O::gt0(flux[ID]) ? (flux[ID] * qleft[IV]) : (flux[ID] * qright[IV]);
+  flux[IV] = flux[ID] * (O::gt0(flux[ID]) ? qleft[IV] : qright[IV]);  // one product, either way
 }
 
 template <typename Real>
