@@ -75,7 +75,7 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
   const double dcen = O::half(qp - qm);
   if (O::le0(dlft * drgt)) return;  // limited to zero
   const bool neg = !O::ge0(dcen);   // dsgn = -1
-  const double al = fabs(dlft), ar = fabs(drgt), ac = fabs(dcen);
+  const double al = rabs(dlft), ar = rabs(drgt), ac = rabs(dcen);
   const bool use_l = picks_first_min(al, ar);
   const double slop = use_l ? al : ar;
   if (picks_first_min(slop, ac)) {

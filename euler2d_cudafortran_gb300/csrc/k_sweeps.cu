@@ -200,7 +200,7 @@ __global__ void k_fluxes_v2(Hydro<Real> h, Field<Real> q, StepDt<Real> sd, Ctl* 
 template <typename Real>
 __device__ __forceinline__ Real new_state_checks(const Hydro<Real>& h, int i, int j, const Real un[4], Ctl* ctl,
                                                  bool want_dt) {
-  if (!(un[ID] > Real(0)) || !isfinite(un[ID])) atomicOr(&ctl->health, 2u);
+  if (bad_density(un[ID])) atomicOr(&ctl->health, 2u);
   if (want_dt && i <= h.isize - 4 && j <= h.jsize - 4) return cell_invdt(h, un);
   return Real(0);
 }

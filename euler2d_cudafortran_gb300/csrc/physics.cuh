@@ -110,7 +110,26 @@ struct Field {
   }
 };
 
+// |a| (the sign bit cleared; for double on the integer pipe, like the other
+// cheap operations of Ops<double>).
 template <typename Real> __device__ __forceinline__ Real rabs(Real a) { return fabs(a); }
+#ifndef E2D_FP64_NATIVE
+template <> __device__ __forceinline__ double rabs<double>(double a) {
+  return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffll);
+}
+#endif
+
+// A new density that is not a positive finite number (the health check of the
+// update; for double decided on the integer pipe).
+__device__ __forceinline__ bool bad_density(float r) { return !(r > 0.0f) || !isfinite(r); }
+__device__ __forceinline__ bool bad_density(double r) {
+#ifdef E2D_FP64_NATIVE
+  return !(r > 0.0) || !isfinite(r);
+#else
+  const long long b = __double_as_longlong(r);
+  return b <= 0 || b >= 0x7ff0000000000000ll;  // -0, negative, +0, or +inf / NaN
+#endif
+}
 
 // eos + computePrimitives, serial_ref/m_utils.f90:15-29 and 35-64, without the
 // sound speed (unused by every caller except compute_dt).
@@ -247,7 +266,7 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
     const Real qr = O::div((O::twice(wwr) * wwr) * wwr, (wwr * wwr) + cr);
     const Real usl = ul - O::div(pold - pl, wwl);
     const Real usr = ur + O::div(pold - pr, wwr);
-    const Real delp = O::max(O::div(qr * ql, qr + ql) * (usl - usr), -pold);
+    const Real delp = O::max(O::div(qr * ql, qr + ql) * (usl - usr), O::neg_if(pold, true));
     pold = pold + delp;
     conv = rabs(O::div(delp, pold + h.smallpp));
     iter = iter + 1;

@@ -180,7 +180,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
           if (ghost_source(g, h.nx, type) == i) {
 #pragma unroll
             for (int v = 0; v < 4; ++v)
-              out.at(v, j, g) = un[v] * ((type == 1 && v == IU) ? Real(-1.0) : Real(1.0));
+              out.at(v, j, g) = Ops<Real>::neg_if(un[v], type == 1 && v == IU);  // reflective: flip u
           }
         }
       }
@@ -192,23 +192,23 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
           if (ghost_source(g, h.ny, type) == j) {
 #pragma unroll
             for (int v = 0; v < 4; ++v)
-              out.at(v, g, i) = un[v] * ((type == 1 && v == IV) ? Real(-1.0) : Real(1.0));
+              out.at(v, g, i) = Ops<Real>::neg_if(un[v], type == 1 && v == IV);  // reflective: flip v
           }
         }
       }
     }
-    if (!(un[ID] > Real(0)) || !isfinite(un[ID])) atomicOr(health, 2u);
+    if (bad_density(un[ID])) atomicOr(health, 2u);
     if (want_dt && i <= h.isize - 4 && j <= h.jsize - 4) m = Ops<Real>::max(m, cell_invdt(h, un));
   }
   if (want_dt) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    for (int o = 16; o > 0; o >>= 1) m = Ops<Real>::max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0) red[tid >> 5] = m;
     __syncthreads();
     if (tid < 32) {
       m = (tid < NT / 32) ? red[tid] : Real(0);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      for (int o = 16; o > 0; o >>= 1) m = Ops<Real>::max(m, __shfl_xor_sync(0xffffffffu, m, o));
     }
   }
   return m;
