@@ -81,13 +81,13 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
   if (picks_first_min(slop, ac)) {
     // slope = dsgn * |dlft| or dsgn * |drgt|
     const double x = use_l ? dlft : drgt;
-    const double g = ((!O::ge0(x)) != neg) ? -sb : sb;  // dsgn * sign(x) * sb
+    const double g = O::neg_if(sb, (!O::ge0(x)) != neg);  // dsgn * sign(x) * sb
     const double sg = mc ? O::twice(g) : g;              // st * g, st = 2 (MC) or 1
     if (use_l) { qbar += sg; qmbar -= sg; }
     else { qpbar += sg; qbar -= sg; }
   } else {
     // slope = dsgn * |dcen| = dcen
-    const double g = O::half(((!O::ge0(dcen)) != neg) ? -sb : sb);
+    const double g = O::half(O::neg_if(sb, (!O::ge0(dcen)) != neg));
     qpbar += g;
     qmbar -= g;
   }
@@ -129,7 +129,7 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
   for (int v = 0; v < 4; ++v) {
     const double hq = O::half(qfb[v]);
     qb[v] += qfb[v];
-    dqb[v] += PLUS ? hq : -hq;
+    dqb[v] += O::neg_if(hq, !PLUS);
     sb[v] += dtd * hq;
     dtdb += s[v] * hq;
   }
@@ -201,7 +201,7 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
       const double rq = O::div(rob, d);
       rlb += rq * (SL - ul); SLb += rq * rl; ulb -= rq * rl;
       const double nEb = O::div(etotob, d);
-      const double db = -(rq * ro + nEb * etoto);  // d(ro, etoto)/d(d)
+      const double db = O::neg_if(rq * ro + nEb * etoto, true);  // d(ro, etoto)/d(d)
       SLb += nEb * etotl; ulb -= nEb * etotl; etotlb += nEb * (SL - ul);
       plb -= nEb * ul; ulb -= nEb * pl; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
       SLb += db; ustarb -= db;
@@ -212,7 +212,7 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
       const double rq = O::div(rob, d);
       rrb += rq * (SR - ur); SRb += rq * rr; urb -= rq * rr;
       const double nEb = O::div(etotob, d);
-      const double db = -(rq * ro + nEb * etoto);
+      const double db = O::neg_if(rq * ro + nEb * etoto, true);
       SRb += nEb * etotr; urb -= nEb * etotr; etotrb += nEb * (SR - ur);
       prb -= nEb * ur; urb -= nEb * pr; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
       SRb += db; ustarb -= db;

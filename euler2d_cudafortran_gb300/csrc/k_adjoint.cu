@@ -294,7 +294,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       }
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const double g = (type == 1 && v == flip) ? -ub[v] : ub[v];
+        const double g = Ops<double>::neg_if(ub[v], type == 1 && v == flip);
         if (g != 0.0) atomicAdd(&ubn.at(v, sj, si), g);
       }
     }
