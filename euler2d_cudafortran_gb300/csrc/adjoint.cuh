@@ -21,11 +21,11 @@ __device__ __forceinline__ bool picks_first_max(double a, double b) { return emu
 __device__ __forceinline__ bool picks_first_min(double a, double b) { return emul::ord(a) < emul::ord(b); }
 
 // computePrimitives (serial_ref/m_utils.f90:35-64) reverse: qb (adjoint of
-// r, p, u, v) -> ub (adjoint of rho, E, rho u, rho v).
-__device__ __forceinline__ void primitives_rev(const Hydro<double>& h, const double u[4], const double qb[4],
-                                               double ub[4]) {
-  const double r = O::max(u[ID], h.smallr);
-  const double uu = O::div(u[IU], r), vv = O::div(u[IV], r);
+// r, p, u, v) -> ub (adjoint of rho, E, rho u, rho v), given the forward
+// primitives q of the same cell (r = q[ID], u = q[IU], v = q[IV]).
+__device__ __forceinline__ void primitives_rev_q(const Hydro<double>& h, const double u[4], const double q[4],
+                                                 const double qb[4], double ub[4]) {
+  const double r = q[ID], uu = q[IU], vv = q[IV];
   const double eken = O::half(uu * uu + vv * vv);
   const double eu = O::div(u[IP], r);
   const double e = eu - eken;
@@ -47,6 +47,14 @@ __device__ __forceinline__ void primitives_rev(const Hydro<double>& h, const dou
   ub[IV] += O::div(ubv, r);
   rb -= O::div(ubu * uu + ubv * vv, r);
   if (picks_first_max(u[ID], h.smallr)) ub[ID] += rb;
+}
+
+// The same, recomputing the primitives from u.
+__device__ __forceinline__ void primitives_rev(const Hydro<double>& h, const double u[4], const double qb[4],
+                                               double ub[4]) {
+  const double r = O::max(u[ID], h.smallr);
+  const double q[4] = {r, 0.0, O::div(u[IU], r), O::div(u[IV], r)};  // ID, IP (unused), IU, IV
+  primitives_rev_q(h, u, q, qb, ub);
 }
 
 // The compute_dt term of one cell (serial_ref/m_run.f90:278-281) reverse.

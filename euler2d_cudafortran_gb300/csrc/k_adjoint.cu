@@ -269,9 +269,10 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       any |= t != 0.0;
     }
     if (any) {
+      double qf[4];  // the forward primitives, still in the box
 #pragma unroll
-      for (int v = 0; v < 4; ++v) u[v] = un.at(v, gj, gi);
-      adj::primitives_rev(h, u, qb, ub);
+      for (int v = 0; v < 4; ++v) { u[v] = un.at(v, gj, gi); qf[v] = sq[v * NBOX + k]; }
+      adj::primitives_rev_q(h, u, qf, qb, ub);
     }
     if (xin && yin) {
       // own interior cells of this tile also carry Ubar' through U' = U + ...
