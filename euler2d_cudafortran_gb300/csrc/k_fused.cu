@@ -16,6 +16,8 @@
 //      next step's CFL maximum (block max + atomic max into a run slot).
 // Primitives, slopes, face states and fluxes never leave shared memory.
 #include <cuda.h>
+
+#include <algorithm>
 #include "sync.cuh"
 #include "tile.cuh"
 
@@ -104,19 +106,146 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
   }
 }
 
+#ifndef E2D_FUSED_PERSISTENT
+#define E2D_FUSED_PERSISTENT 0
+#endif
+
+// Persistent variant (FP64): a grid of resident CTAs walks the tiles with a
+// fixed stride.  The box of a CTA's next tile is loaded by TMA into the slope
+// region as soon as the face phase of the current tile has ended (the slopes
+// and sources are no longer read then), so the load lands while the update
+// phase runs; the primitives phase of the next tile reads it from there.
+// One mbarrier, one phase per load; every wait is bounded.
+template <typename Real>
+__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
+    k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
+                       StepDt<Real> sd, Ctl* ctl, int fill_ghosts, int ntx, int ntiles) {
+  using C = typename FusedTile<Real>::C;
+  static_assert(8ull * C::RY * C::RX >= 4ull * C::BYs * C::BXs, "the next box fits in the slope region");
+  static_assert((C::d_off * sizeof(Real)) % 128 == 0, "TMA destination alignment of the slope region");
+  extern __shared__ unsigned char smem_raw[];
+  Real* base = reinterpret_cast<Real*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  unsigned char* tail = reinterpret_cast<unsigned char*>(base + C::n_real);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tail);
+  int* face_counter = reinterpret_cast<int*>(tail + 8);
+  Real* red = reinterpret_cast<Real*>(tail + 16);
+  Real* sdt = red + 32;
+  Real* dreg = base + C::d_off;
+  const int tid = threadIdx.x;
+  const uint32_t bar_a = smem_u32(bar);
+  auto issue = [&](int t, Real* dst) {  // thread 0: the box of tile t into dst
+    const int i0 = GW + (t % ntx) * C::TX, j0 = GW + (t / ntx) * C::TY;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(C::box_bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
+        : "memory");
+  };
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *face_counter = 0;
+    const Real dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? h.cfl / *inv_slot<Real>(ctl, sd.rd_slot) : sd.dt_value;
+    sdt[0] = dt0;
+    sdt[1] = dt0 / h.dx;
+    sdt[2] = dt0 / h.dy;
+    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, base + C::q_off);
+  }
+  __syncthreads();
+  const bool want_dt = sd.wr_slot >= 0;
+  Real mmax = Real(0);
+  uint32_t parity = 0;
+  bool first = true;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const bool ok = mbar_wait(bar_a, parity, kTmaWaitCycles);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(&ctl->health, 4u);
+      return;
+    }
+    parity ^= 1;
+    const int next = t + gridDim.x;
+    const int i0 = GW + (t % ntx) * C::TX, j0 = GW + (t / ntx) * C::TY;
+    auto prefetch = [&]() {
+      if (tid == 0 && next < ntiles) issue(next, dreg);
+    };
+    const Real m = tile_compute<Real, C>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2],
+                                         fill_ghosts != 0, want_dt, &ctl->health, first ? nullptr : dreg, prefetch);
+    if (tid == 0) {
+      mmax = Ops<Real>::max(mmax, m);
+      *face_counter = 0;
+    }
+    __syncthreads();  // this tile's shared data consumed; the counter reset is visible
+    first = false;
+  }
+  if (tid == 0) {
+    const Real dt = sdt[0];
+    if (blockIdx.x == 0) {
+      if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
+      if (sd.inv_log && sd.rd_slot >= 0) sd.inv_log[sd.log_index] = *inv_slot<Real>(ctl, sd.rd_slot);
+      if (!isfinite(dt)) atomicOr(&ctl->health, 1u);
+    }
+    if (want_dt) {
+      if (sd.rd_slot >= 0) mmax = Ops<Real>::max(mmax, *inv_slot<Real>(ctl, sd.rd_slot));
+      atomic_max_slot_ptr<Real>(inv_slot<Real>(ctl, sd.wr_slot), mmax);
+    }
+  }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Resident CTAs per SM x SMs of the current device (the persistent grid).
+template <typename Real>
+int persistent_grid() {
+  static int grid[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!grid[dev]) {
+    using C = typename FusedTile<Real>::C;
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real>, C::NT, C::bytes);
+    grid[dev] = std::max(1, sms * std::max(1, per_sm));
+  }
+  return grid[dev];
+}
 
 // Dynamic shared memory of the tile, and the largest shared-memory carveout
 // so that as many CTAs as the launch bounds ask for fit on an SM.
 template <typename Real>
 bool set_fused_attributes() {
   using C = typename FusedTile<Real>::C;
-  return cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
-             cudaSuccess &&
-         cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
+  bool ok = cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
+  if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT)
+    ok = ok &&
+         cudaFuncSetAttribute(k_fused_persistent<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)C::bytes) == cudaSuccess &&
+         cudaFuncSetAttribute(k_fused_persistent<Real>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
+         persistent_grid<Real>() > 0;  // sized here, outside any stream capture
+  return ok;
+}
+
+template <typename Real>
+void launch_fused_tm(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out, StepDt<Real> sd,
+                     Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+  using C = typename FusedTile<Real>::C;
+  const int ntx = (h.nx + C::TX - 1) / C::TX, nty = (h.ny + C::TY - 1) / C::TY;
+  if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT) {
+    const int grid = std::min(ntx * nty, persistent_grid<Real>());
+    k_fused_persistent<Real><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0, ntx,
+                                                           ntx * nty);
+  } else {
+    k_fused<Real><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0);
+  }
 }
 
 EncodeTiledFn get_encode_fn() {
@@ -173,9 +302,7 @@ void fused_plan_destroy(FusedPlan* p) { delete p; }
 template <typename Real>
 void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in, Field<Real> out,
                   StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
-  using C = typename FusedTile<Real>::C;
-  dim3 g((h.nx + C::TX - 1) / C::TX, (h.ny + C::TY - 1) / C::TY);
-  k_fused<Real><<<g, C::NT, C::bytes, s>>>(plan->tm[in_is_u2 ? 1 : 0], h, in, out, sd, ctl, fill_ghosts ? 1 : 0);
+  launch_fused_tm<Real>(plan->tm[in_is_u2 ? 1 : 0], h, in, out, sd, ctl, fill_ghosts, s);
 }
 
 template <typename Real>
@@ -192,10 +319,7 @@ bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out) {
 template <typename Real>
 void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in, Field<Real> out, StepDt<Real> sd,
                       Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
-  using C = typename FusedTile<Real>::C;
-  dim3 g((h.nx + C::TX - 1) / C::TX, (h.ny + C::TY - 1) / C::TY);
-  k_fused<Real><<<g, C::NT, C::bytes, s>>>(*reinterpret_cast<const CUtensorMap*>(map.bytes), h, in, out, sd, ctl,
-                                           fill_ghosts ? 1 : 0);
+  launch_fused_tm<Real>(*reinterpret_cast<const CUtensorMap*>(map.bytes), h, in, out, sd, ctl, fill_ghosts, s);
 }
 
 template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*);

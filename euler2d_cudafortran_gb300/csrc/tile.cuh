@@ -57,11 +57,22 @@ __device__ __forceinline__ void atomic_max_slot_ptr<float>(float* slot, float m)
 // Phases 2-5 for the tile at (i0, j0); all threads call it after the box is
 // in base[q_off..].  *face_counter must be 0.  Returns, in thread 0, the
 // block maximum of the CFL term of the new state (0 when !want_dt).
-template <typename Real, class C>
+// A no-op for the after-faces hook of tile_compute.
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+// box_src (optional): where the conservative box was loaded, when not in
+// place at q_off (it is then read into q_off); after_faces: run by every
+// thread right after the barrier that ends the face phase, when the slope
+// and source regions are no longer read (a persistent caller prefetches the
+// next box there).
+template <typename Real, class C, class Hook = NoHook>
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
                                              int i0, int j0, const Field<Real>& in, const Field<Real>& out,
                                              Real dtdx, Real dtdy, bool fill_ghosts, bool want_dt,
-                                             unsigned* health) {
+                                             unsigned* health, const Real* box_src = nullptr,
+                                             Hook after_faces = Hook()) {
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, BXs = C::BXs, BYs = C::BYs, RX = C::RX, RY = C::RY;
   Real* sq = base + C::q_off;
   Real* sdq = base + C::d_off;
@@ -70,11 +81,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   Real* sfy = base + C::fy_off;
   const int tid = threadIdx.x;
 
-  // ---- primitives of the whole box, in place (computePrimitives)
+  // ---- primitives of the whole box (computePrimitives), in place unless
+  // the box was loaded elsewhere
+  const Real* src = box_src ? box_src : sq;
   for (int k = tid; k < BXs * BYs; k += NT) {
     Real u[4], q[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) u[v] = sq[v * BXs * BYs + k];
+    for (int v = 0; v < 4; ++v) u[v] = src[v * BXs * BYs + k];
     primitives(h, u, q);
 #pragma unroll
     for (int v = 0; v < 4; ++v) sq[v * BXs * BYs + k] = q[v];
@@ -156,6 +169,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
   }
   __syncthreads();
+  after_faces();
 
   // ---- updateHydro + ghost copies + next-step CFL maximum
   Real m = Real(0);
