@@ -107,11 +107,11 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
 }
 
 #ifndef E2D_FUSED_PERSISTENT
-#define E2D_FUSED_PERSISTENT 0
+#define E2D_FUSED_PERSISTENT 1
 #endif
 
-// Persistent variant (FP64): a grid of resident CTAs walks the tiles with a
-// fixed stride.  The box of a CTA's next tile is loaded by TMA into the slope
+// Persistent variant (FP64, the default; E2D_FUSED_PERSISTENT=0 selects one
+// CTA per tile): a grid of resident CTAs walks the tiles with a fixed stride.  The box of a CTA's next tile is loaded by TMA into the slope
 // region as soon as the face phase of the current tile has ended (the slopes
 // and sources are no longer read then), so the load lands while the update
 // phase runs; the primitives phase of the next tile reads it from there.
