@@ -1,0 +1,62 @@
+"""Where the work runs: on a stream the caller owns (e2d_set_stream), and
+step by step with per-step events (e2d_time_steps, the path the benchmark's
+roofline times).  Both must leave bit for bit the states and running CFL
+maximum of the library's default path."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(E, version=0, prec=8):
+    return E.make_params(nx=96, ny=80, gamma0=1.4, cfl=0.8, riemann_solver=E.RIEMANN_HLLC,
+                         implementation_version=version, precision=prec, boundary_type_xmax=2, boundary_type_ymin=3,
+                         boundary_type_ymax=3)
+
+
+@pytest.mark.parametrize("version", [0, 1, 2])
+def test_caller_stream_gives_the_same_states(e2d, version):
+    torch = pytest.importorskip("torch")
+    p = _params(e2d, version)
+    with e2d.HydroRun(p) as a:
+        a.init_implode()
+        da = a.advance(0, 12)
+        a.make_boundaries(0)
+        ua = a.final_state(12)
+    s = torch.cuda.Stream()
+    with e2d.HydroRun(p) as b:
+        b.set_stream(s.cuda_stream)
+        b.init_implode()
+        db = b.advance(0, 7)  # graph captured on the caller's stream
+        for n in range(7, 12):  # then the reference's per-call loop on it
+            db = np.append(db, b.compute_dt(n % 2))
+            b.godunov_unsplit(n, db[-1])
+        # The per-call steps leave the ghosts of their output to the next
+        # make_boundaries (serial_ref/m_run.f90:224); the fused advance writes them in
+        # the update: fill them on both runs before comparing whole arrays.
+        b.make_boundaries(0)
+        s.synchronize()
+        ub = b.final_state(12)
+        b.set_stream(None)
+    assert np.array_equal(ua, ub)
+    assert np.array_equal(da, db)
+
+
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+def test_time_steps_leaves_the_advance_state(e2d, prec):
+    p = _params(e2d, 0, prec)
+    with e2d.HydroRun(p) as a:
+        a.init_implode()
+        a.advance(0, 3)
+        a.advance(3, 9)
+        ua, inv_a = a.final_state(12), a.invdt()
+    with e2d.HydroRun(p) as b:
+        b.init_implode()
+        b.advance(0, 3)
+        ms = b.time_steps(3, 9)
+        ub, inv_b = b.final_state(12), b.invdt()
+        assert np.all(ms > 0)
+        b.advance(12, 2)  # carries on from the timed steps
+        assert b.health() == 0
+    assert np.array_equal(ua, ub)
+    assert inv_a == inv_b
