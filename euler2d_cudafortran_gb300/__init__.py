@@ -564,7 +564,8 @@ def selftest_wait(limit_cycles: int = 1 << 24):
 
 def selftest_arith(op: int, mode: int, n: int, seed: int = 1, rates: bool = False):
     """Bitwise check of the integer-pipe division (op 0) / square root (op 1)
-    against the hardware on n inputs; returns (mismatches, first_bad[4], rates)."""
+    against the hardware, or of the exponent-test pressure floor (op 2) against
+    the product and maximum, on n inputs; returns (mismatches, first_bad[4], rates)."""
     bad = ctypes.c_ulonglong()
     first = (ctypes.c_double * 4)()
     em, na = ctypes.c_double(), ctypes.c_double()

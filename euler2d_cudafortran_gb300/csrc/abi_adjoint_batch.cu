@@ -48,6 +48,7 @@ struct e2d_adjoint_batch {
   BatchProb<double>* d_fwd = nullptr;  // forward ping-pong, work-list order
   BatchProb<double>* d_seg = nullptr;  // [2][K - 1][nprob]: segment set, state j -> j + 1
   int fwd_tiles = 0, fwd_grid = 0, rev_tiles = 0, nparts = 64;
+  bool square = false;  // every problem has dx == dy
   Ctl* ctls = nullptr;
   double *dt_log = nullptr, *inv_log = nullptr, *dtbar_log = nullptr;
   double* J = nullptr;
@@ -192,6 +193,7 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
       }
   }
   b->fwd_tiles = ft;
+  b->square = std::all_of(fw.begin(), fw.end(), [](const BatchProb<double>& F) { return F.h.dx == F.h.dy; });
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   b->fwd_grid = std::max(1, std::min(ft, sms * std::max(1, batch_resident_per_sm<double>(0))));
@@ -225,6 +227,7 @@ BatchLaunch<double> step_launch(const e2d_adjoint_batch* b, const BatchProb<doub
   L.rd = -1;
   L.wr = -1;
   L.dt_log = nullptr;
+  L.square = b->square;
   return L;
 }
 

@@ -36,6 +36,7 @@ struct e2d_batch {
   int dtlog_cap = 0;
   int variant = 0, mult = 1, order = 1;  // schedule
   int total_tiles = 0, grid = 0;
+  bool square = false;  // every problem has dx == dy
   int cur_slot = 0;
   bool folded = false;
   cudaStream_t stream = nullptr;
@@ -97,6 +98,7 @@ int build_worklist(e2d_batch* b) {
     t += P.ntx * P.nty;
   }
   b->total_tiles = t;
+  b->square = std::all_of(probs.begin(), probs.end(), [](const BatchProb<Real>& P) { return P.h.dx == P.h.dy; });
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -130,6 +132,7 @@ void enqueue(e2d_batch* b, int nStep0, int nsteps, int slot0, bool seed) {
     L.grid = b->grid;
     L.ctls = b->ctls;
     L.dt_log = static_cast<Real*>(b->d_dtlog) + (size_t)k * b->nprob;
+    L.square = b->square;
     launch_batch_step<Real>(b->variant, L, b->stream);
   }
 }

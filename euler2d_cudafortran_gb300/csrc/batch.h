@@ -24,6 +24,7 @@ struct BatchLaunch {
   Real* dt_log;   // device, nprob entries for this step by problem index (may be null)
   const Real* dt_src = nullptr;  // if set: step with these logged dt (by problem index), no CFL fold
   Real* inv_log = nullptr;       // if set: receives each problem's running CFL maximum before the step
+  bool square = false;           // every problem has dx == dy (selects the kernel that shares face sources)
 };
 
 // Tile shapes: variant 0 = 32 x 15 cells (256 threads), 1 = 32 x 7 (128 threads).

@@ -8,6 +8,8 @@
 // (from the problem's running CFL maximum) and its own ghost rules, and
 // folds the next step's CFL maximum into the problem's own slot.  The box is
 // loaded with coalesced plain loads because every problem has its own array.
+#include <algorithm>
+
 #include "batch.h"
 #include "tile.cuh"
 
@@ -15,7 +17,9 @@ namespace e2d {
 
 namespace {
 
-template <typename Real, class C, int MINB>
+// SQ: every problem of the launch has dx == dy (the shared face source term
+// of tile_compute).
+template <typename Real, class C, int MINB, bool SQ>
 __global__ void __launch_bounds__(C::NT, MINB)
     k_batch_step(const BatchProb<Real>* __restrict__ probs, int nprob, int total_tiles, int parity, int rd, int wr,
                  Ctl* ctls, Real* dt_log, const Real* dt_src, Real* inv_log) {
@@ -63,7 +67,7 @@ __global__ void __launch_bounds__(C::NT, MINB)
       sq[k] = (gi < sh.isize && gj < sh.jsize) ? in.at(v, gj, gi) : Real(0);
     }
     __syncthreads();
-    Real m = tile_compute<Real, C>(sh, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2], true, wr >= 0,
+    Real m = tile_compute<Real, C, SQ>(sh, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2], true, wr >= 0,
                                    &ctls[id].health);
     if (tid == 0) {
       if (stile == 0) {
@@ -82,22 +86,30 @@ __global__ void __launch_bounds__(C::NT, MINB)
 
 template <typename Real, class C, int MINB>
 struct Variant {
-  static int resident_per_sm() {
+  template <bool SQ>
+  static int resident_sq() {
     int n = 0;
-    if (cudaFuncSetAttribute(k_batch_step<Real, C, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_batch_step<Real, C, MINB, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)C::bytes) != cudaSuccess ||
-        cudaFuncSetAttribute(k_batch_step<Real, C, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        cudaFuncSetAttribute(k_batch_step<Real, C, MINB, SQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<Real, C, MINB>, C::NT, C::bytes) !=
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<Real, C, MINB, SQ>, C::NT, C::bytes) !=
             cudaSuccess) {
       cudaGetLastError();
       return 0;
     }
     return n;
   }
+  // CTAs of either instantiation that fit on an SM (the persistent grid is
+  // sized by it, so it must hold for the one launched).
+  static int resident_per_sm() { return std::min(resident_sq<false>(), resident_sq<true>()); }
   static void launch(const BatchLaunch<Real>& L, cudaStream_t s) {
-    k_batch_step<Real, C, MINB><<<L.grid, C::NT, C::bytes, s>>>(L.probs, L.nprob, L.total_tiles, L.parity, L.rd,
-                                                                L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+    if (L.square)
+      k_batch_step<Real, C, MINB, true><<<L.grid, C::NT, C::bytes, s>>>(
+          L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+    else
+      k_batch_step<Real, C, MINB, false><<<L.grid, C::NT, C::bytes, s>>>(
+          L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
   }
 };
 

@@ -43,7 +43,8 @@ template <typename Real> struct FusedTile;
 template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, 256>; };
 template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 
-template <typename Real>
+// SQ: dx == dy (the shared face source term of tile_compute).
+template <typename Real, bool SQ>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
             StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
@@ -91,8 +92,8 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     return;
   }
   const bool want_dt = sd.wr_slot >= 0;
-  Real m = tile_compute<Real, C>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2], fill_ghosts != 0,
-                                 want_dt, &ctl->health);
+  Real m = tile_compute<Real, C, SQ>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2],
+                                     fill_ghosts != 0, want_dt, &ctl->health);
   if (tid == 0) {
     if (blockIdx.x == 0 && blockIdx.y == 0) {
       if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
@@ -109,6 +110,9 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
 #ifndef E2D_FUSED_PERSISTENT
 #define E2D_FUSED_PERSISTENT 1
 #endif
+#ifndef E2D_SQ_TRACE
+#define E2D_SQ_TRACE 1
+#endif
 
 // Persistent variant (FP64, the default; E2D_FUSED_PERSISTENT=0 selects one
 // CTA per tile): a grid of resident CTAs walks the tiles with a fixed stride.  The box of a CTA's next tile is loaded by TMA into the slope
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
 // and sources are no longer read then), so the load lands while the update
 // phase runs; the primitives phase of the next tile reads it from there.
 // One mbarrier, one phase per load; every wait is bounded.
-template <typename Real>
+template <typename Real, bool SQ>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
                        StepDt<Real> sd, Ctl* ctl, int fill_ghosts, int ntx, int ntiles) {
@@ -171,7 +175,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     auto prefetch = [&]() {
       if (tid == 0 && next < ntiles) issue(next, dreg);
     };
-    const Real m = tile_compute<Real, C>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2],
+    const Real m = tile_compute<Real, C, SQ>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2],
                                          fill_ghosts != 0, want_dt, &ctl->health, first ? nullptr : dreg, prefetch);
     if (tid == 0) {
       mmax = Ops<Real>::max(mmax, m);
@@ -199,7 +203,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 // Resident CTAs per SM x SMs of the current device (the persistent grid).
-template <typename Real>
+template <typename Real, bool SQ>
 int persistent_grid() {
   static int grid[64] = {0};
   int dev = 0;
@@ -209,7 +213,7 @@ int persistent_grid() {
     using C = typename FusedTile<Real>::C;
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real>, C::NT, C::bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real, SQ>, C::NT, C::bytes);
     grid[dev] = std::max(1, sms * std::max(1, per_sm));
   }
   return grid[dev];
@@ -217,35 +221,54 @@ int persistent_grid() {
 
 // Dynamic shared memory of the tile, and the largest shared-memory carveout
 // so that as many CTAs as the launch bounds ask for fit on an SM.
-template <typename Real>
-bool set_fused_attributes() {
+template <typename Real, bool SQ>
+bool set_fused_attributes_sq() {
   using C = typename FusedTile<Real>::C;
-  bool ok = cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
+  bool ok = cudaFuncSetAttribute(k_fused<Real, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
                 cudaSuccess &&
-            cudaFuncSetAttribute(k_fused<Real>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            cudaFuncSetAttribute(k_fused<Real, SQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
   if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT)
     ok = ok &&
-         cudaFuncSetAttribute(k_fused_persistent<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+         cudaFuncSetAttribute(k_fused_persistent<Real, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)C::bytes) == cudaSuccess &&
-         cudaFuncSetAttribute(k_fused_persistent<Real>, cudaFuncAttributePreferredSharedMemoryCarveout,
+         cudaFuncSetAttribute(k_fused_persistent<Real, SQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
                               (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
-         persistent_grid<Real>() > 0;  // sized here, outside any stream capture
+         persistent_grid<Real, SQ>() > 0;  // sized here, outside any stream capture
   return ok;
 }
 
 template <typename Real>
-void launch_fused_tm(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out, StepDt<Real> sd,
+bool set_fused_attributes() {
+  return set_fused_attributes_sq<Real, false>() && set_fused_attributes_sq<Real, true>();
+}
+
+template <typename Real, bool SQ>
+void launch_fused_sq(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out, StepDt<Real> sd,
                      Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
   using C = typename FusedTile<Real>::C;
   const int ntx = (h.nx + C::TX - 1) / C::TX, nty = (h.ny + C::TY - 1) / C::TY;
   if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT) {
-    const int grid = std::min(ntx * nty, persistent_grid<Real>());
-    k_fused_persistent<Real><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0, ntx,
-                                                           ntx * nty);
+    const int grid = std::min(ntx * nty, persistent_grid<Real, SQ>());
+    k_fused_persistent<Real, SQ><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0, ntx,
+                                                               ntx * nty);
   } else {
-    k_fused<Real><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0);
+    k_fused<Real, SQ><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0);
   }
+}
+
+// dx == dy (a square domain of square cells, every benchmark grid) takes the
+// instantiation that forms each cell's face source term once.
+template <typename Real>
+void launch_fused_tm(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out, StepDt<Real> sd,
+                     Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+#if E2D_SQ_TRACE
+  if (h.dx == h.dy) {
+    launch_fused_sq<Real, true>(tm, h, in, out, sd, ctl, fill_ghosts, s);
+    return;
+  }
+#endif
+  launch_fused_sq<Real, false>(tm, h, in, out, sd, ctl, fill_ghosts, s);
 }
 
 EncodeTiledFn get_encode_fn() {

@@ -1,11 +1,14 @@
 // k_selftest.cu -- on-device check of the emulated double division and square
 // root (emul64.cuh) against the hardware operations, bit for bit, plus their
-// throughput.  Exposed as e2d_selftest_arith for the GPU tests.
+// throughput, and of the exponent-test pressure floor (physics.cuh) against
+// the product and maximum it stands for.  Exposed as e2d_selftest_arith for
+// the GPU tests.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "../../include/euler2d_gb300.h"
 #include "emul64.cuh"
+#include "physics.cuh"
 #include "sync.cuh"
 
 namespace {
@@ -32,14 +35,37 @@ __device__ bool same(double x, double y) {
   return a == b;
 }
 
-// op 0: division, op 1: square root.  Modes 0-2 as rand_double; mode 4 signed
-// zeros and small integers; mode 3 builds
+// op 0: division, op 1: square root, op 2: the pressure floor max(a, b*c)
+// (against the emulated maximum of the hardware product).  Modes 0-2 as
+// rand_double; mode 4 signed zeros and small integers; mode 3 builds
 // operands whose exact result lies within one part in 2^60 of a rounding
-// boundary (quotient q + 1/2 ulp times b, or (q + 1/2 ulp)^2).
+// boundary (quotient q + 1/2 ulp times b, or (q + 1/2 ulp)^2), and for op 2
+// an a within two binades of b*c, either sign.
 __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned long long* bad, double* first) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const uint64_t r1 = mix64(seed ^ (uint64_t)k), r2 = mix64(r1 + 0x1234567ull);
     double a, b = 1.0;
+    if (op == 2) {
+      const uint64_t r3 = mix64(r2 + 0x7654321ull);
+      b = rand_double(r2, mode == 0 ? 0 : mode == 4 ? 2 : 1);
+      const double c = rand_double(r3, mode == 0 ? 0 : 2);
+      if (mode == 3) {  // a = +-(b*c) with its exponent moved by -2..2 and a fresh mantissa
+        const long long pb = __double_as_longlong(__dmul_rn(b, c));
+        const long long e = ((pb >> 52) & 0x7ff) + (long long)(r1 % 5) - 2;
+        a = (e > 0 && e < 2047) ? __longlong_as_double((long long)(r1 & 0x800fffffffffffffull) | (e << 52)) : 1.0;
+      } else if (mode == 4) {
+        a = (r1 & 2) ? 0.0 : rand_double(r1, 2);
+        a = (r1 & 1) ? -a : a;
+      } else {
+        a = rand_double(r1, mode);
+      }
+      const double x = e2d::floor_prod<double>(a, b, c);
+      const double y = e2d::emul::max_i(a, __dmul_rn(b, c));
+      if (!same(x, y)) {
+        if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
+      }
+      continue;
+    }
     if (mode < 3) {
       a = rand_double(r1, mode);
       b = rand_double(r2, mode);
@@ -136,7 +162,7 @@ extern "C" int e2d_selftest_wait(long long limit_cycles, int* arrived_completed,
 extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* first_bad, double* emulated_per_s,
                                   double* native_per_s) {
-  if ((op != 0 && op != 1) || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
+  if (op < 0 || op > 2 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
@@ -160,7 +186,7 @@ extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long l
   k_check<<<blocks, threads>>>(op, mode, n, seed, d_bad, d_first);
   cudaMemcpy(mismatches, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   if (first_bad) cudaMemcpy(first_bad, d_first, 4 * sizeof(double), cudaMemcpyDeviceToHost);
-  if (emulated_per_s && native_per_s) {
+  if (emulated_per_s && native_per_s && op < 2) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -119,6 +119,29 @@ template <> __device__ __forceinline__ double rabs<double>(double a) {
 }
 #endif
 
+// max(a, b*c), the pressure floors of eos and the Riemann solvers (b a
+// density, c = smallp).  For double, when a is a positive normal number with
+// a >= 2^(ea-1023) >= 2^(eb+ec-2044) > b*c (ea, eb, ec the biased exponent
+// fields; the bound holds for subnormal b or c too), the maximum is a whatever
+// b*c rounds to, and the product is not formed: an exponent test on the
+// integer pipe.  Other operands (a near the floor, zero, negative, NaN or
+// infinite; b or c not finite) take the IEEE product and maximum.
+#ifndef E2D_PFLOOR_EXP
+#define E2D_PFLOOR_EXP 1
+#endif
+template <typename Real> __device__ __forceinline__ Real floor_prod(Real a, Real b, Real c) {
+  return Ops<Real>::max(a, b * c);
+}
+#if !defined(E2D_FP64_NATIVE) && E2D_PFLOOR_EXP
+template <> __device__ __forceinline__ double floor_prod<double>(double a, double b, double c) {
+  const int ha = __double2hiint(a), hb = __double2hiint(b), hc = __double2hiint(c);
+  const bool dominant = (unsigned)(ha - 0x00100000) < 0x7fe00000u && (unsigned)hb < 0x7ff00000u &&
+                        (unsigned)hc < 0x7ff00000u && (ha >> 20) >= (hb >> 20) + (hc >> 20) - 1021;
+  if (dominant) return a;
+  return Ops<double>::max(a, b * c);
+}
+#endif
+
 // A new density that is not a positive finite number (the health check of the
 // update; for double decided on the integer pipe).
 __device__ __forceinline__ bool bad_density(float r) { return !(r > 0.0f) || !isfinite(r); }
@@ -141,7 +164,7 @@ __device__ __forceinline__ void primitives(const Hydro<Real>& h, const Real u[4]
   q[IV] = O::div(u[IV], q[ID]);
   const Real eken = O::half((q[IU] * q[IU]) + (q[IV] * q[IV]));
   const Real e = O::div(u[IP], q[ID]) - eken;
-  q[IP] = O::max((h.gm1 * q[ID]) * e, q[ID] * h.smallp);
+  q[IP] = floor_prod((h.gm1 * q[ID]) * e, q[ID], h.smallp);
 }
 
 // Sound speed of eos (serial_ref/m_utils.f90:27) from primitive q.
@@ -214,15 +237,15 @@ __device__ __forceinline__ void trace_sources(const Hydro<Real>& h, const Real q
 // Face state of trace_unsplit_2d_along_dir, serial_ref/m_utils.f90:218-252:
 // qf = (q -/+ 0.5*dq_dir) + (s*dtd)*0.5, then rho floored at smallr.
 // PLUS selects the XMAX/YMAX faces; dq is the slope along the face normal,
-// dtd = dtdx or dtdy.
-template <typename Real, bool PLUS>
+// dtd = dtdx or dtdy.  PRE: s already holds (s*dtd)*0.5.
+template <typename Real, bool PLUS, bool PRE = false>
 __device__ __forceinline__ void trace_face(const Hydro<Real>& h, const Real q[4], const Real dq[4],
                                            const Real s[4], Real dtd, Real qf[4]) {
   using O = Ops<Real>;
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     const Real a = PLUS ? (q[v] + O::half(dq[v])) : (q[v] - O::half(dq[v]));
-    qf[v] = a + O::half(s[v] * dtd);
+    qf[v] = a + (PRE ? s[v] : O::half(s[v] * dtd));
   }
   qf[ID] = O::max(h.smallr, qf[ID]);
 }
@@ -248,10 +271,10 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
   const Real tol = Real(1e-6f);
   const Real rl = O::max(qleft[ID], h.smallr);
   const Real ul = qleft[IU];
-  const Real pl = O::max(qleft[IP], rl * h.smallp);
+  const Real pl = floor_prod(qleft[IP], rl, h.smallp);
   const Real rr = O::max(qright[ID], h.smallr);
   const Real ur = qright[IU];
-  const Real pr = O::max(qright[IP], rr * h.smallp);
+  const Real pr = floor_prod(qright[IP], rr, h.smallp);
   const Real cl = (h.gamma0 * pl) * rl;
   const Real cr = (h.gamma0 * pr) * rr;
   Real wl = O::sqrt(cl);
@@ -305,7 +328,7 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
                                              const Real qright[4], Real flux[4]) {
   using O = Ops<Real>;
   const Real rl = O::max(qleft[ID], h.smallr);
-  const Real pl = O::max(qleft[IP], rl * h.smallp);
+  const Real pl = floor_prod(qleft[IP], rl, h.smallp);
   const Real ul = qleft[IU];
   const Real hrl = O::half(rl);
   Real ecinl = (hrl * ul) * ul;
@@ -313,7 +336,7 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real etotl = (pl * h.entho) + ecinl;
   const Real ptotl = pl;
   const Real rr = O::max(qright[ID], h.smallr);
-  const Real pr = O::max(qright[IP], rr * h.smallp);
+  const Real pr = floor_prod(qright[IP], rr, h.smallp);
   const Real ur = qright[IU];
   const Real hrr = O::half(rr);
   Real ecinr = (hrr * ur) * ur;

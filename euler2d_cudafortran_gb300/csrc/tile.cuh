@@ -67,7 +67,10 @@ struct NoHook {
 // thread right after the barrier that ends the face phase, when the slope
 // and source regions are no longer read (a persistent caller prefetches the
 // next box there).
-template <typename Real, class C, class Hook = NoHook>
+// SQ (only when dx == dy, so that dtdx == dtdy bit for bit): the source term
+// of a face state, (s*dtdx)*0.5, is the same for the four faces of a cell;
+// the ring pass forms it once and stores it in place of s.
+template <typename Real, class C, bool SQ = false, class Hook = NoHook>
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
                                              int i0, int j0, const Field<Real>& in, const Field<Real>& out,
                                              Real dtdx, Real dtdy, bool fill_ghosts, bool want_dt,
@@ -111,6 +114,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
     slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
     trace_sources(h, qc, dqx, dqy, s);
+    if constexpr (SQ) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) s[v] = Ops<Real>::half(s[v] * dtdx);
+    }
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       sdq[v * RX * RY + kr] = dqx[v];
@@ -139,10 +146,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 1); dq[v] = sdq[v * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
-        trace_face<Real, true>(h, qc, dq, s, dtdx, ql);
+        trace_face<Real, true, SQ>(h, qc, dq, s, dtdx, ql);
 #pragma unroll
         for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 2); dq[v] = sdq[v * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
-        trace_face<Real, false>(h, qc, dq, s, dtdx, qr);
+        trace_face<Real, false, SQ>(h, qc, dq, s, dtdx, qr);
         riemann(h, ql, qr, flux);
 #pragma unroll
         for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = flux[v] * dtdx;
@@ -155,10 +162,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 1, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
-        trace_face<Real, true>(h, qc, dq, s, dtdy, ql);
+        trace_face<Real, true, SQ>(h, qc, dq, s, dtdy, ql);
 #pragma unroll
         for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 2, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
-        trace_face<Real, false>(h, qc, dq, s, dtdy, qr);
+        trace_face<Real, false, SQ>(h, qc, dq, s, dtdy, qr);
         Real t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
         t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
         riemann(h, ql, qr, flux);

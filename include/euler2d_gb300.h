@@ -135,11 +135,14 @@ int e2d_time_steps(e2d_run* h, int nStep0, int nsteps, float* ms);
 int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
 
 /* Self-test of the library's integer-pipe double division (op 0) and square
- * root (op 1) against the hardware operations on n seeded inputs (mode 0 any
- * bit pattern, 1 exponents near 1, 2 exponents within +-400, 3 results next to
- * rounding boundaries, 4 signed zeros and small integers): *mismatches counts results that differ in any bit,
- * first_bad[4] (optional) = a, b, emulated, hardware of the first one; the
- * two rates (optional) are chained operations per second.  Not part of the
+ * root (op 1) against the hardware operations, and of its exponent-test
+ * pressure floor max(a, b*c) (op 2) against the product and maximum, on n
+ * seeded inputs (mode 0 any bit pattern, 1 exponents near 1, 2 exponents
+ * within +-400, 3 results next to rounding boundaries -- for op 2, a within
+ * two binades of b*c --, 4 signed zeros and small integers): *mismatches
+ * counts results that differ in any bit, first_bad[4] (optional) = a, b,
+ * library, reference operation of the first one; the two rates (optional,
+ * ops 0 and 1) are chained operations per second.  Not part of the
  * reference; used by the tests. */
 int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed, unsigned long long* mismatches,
                        double* first_bad, double* emulated_per_s, double* native_per_s);
