@@ -115,9 +115,18 @@ struct Field {
 template <typename Real> __device__ __forceinline__ Real rabs(Real a) { return fabs(a); }
 #ifndef E2D_FP64_NATIVE
 template <> __device__ __forceinline__ double rabs<double>(double a) {
-  return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffll);
+  return emul::from_bits(emul::bits(a) & 0x7fffffffffffffffull);
 }
 #endif
+
+// a*b rounded to nearest, as an instruction the compiler may not move out of
+// the branch that holds it (a multiplication is otherwise free to be
+// computed ahead of the test that makes it unnecessary).
+__device__ __forceinline__ double dmul_kept(double a, double b) {
+  double r;
+  asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+  return r;
+}
 
 // max(a, b*c), the pressure floors of eos and the Riemann solvers (b a
 // density, c = smallp).  For double, when a is a positive normal number with
@@ -134,11 +143,15 @@ template <typename Real> __device__ __forceinline__ Real floor_prod(Real a, Real
 }
 #if !defined(E2D_FP64_NATIVE) && E2D_PFLOOR_EXP
 template <> __device__ __forceinline__ double floor_prod<double>(double a, double b, double c) {
-  const int ha = __double2hiint(a), hb = __double2hiint(b), hc = __double2hiint(c);
+  const int ha = (int)(emul::bits(a) >> 32), hb = (int)(emul::bits(b) >> 32), hc = (int)(emul::bits(c) >> 32);
   const bool dominant = (unsigned)(ha - 0x00100000) < 0x7fe00000u && (unsigned)hb < 0x7ff00000u &&
                         (unsigned)hc < 0x7ff00000u && (ha >> 20) >= (hb >> 20) + (hc >> 20) - 1021;
   if (dominant) return a;
+#if E2D_PFLOOR_EXP == 2
+  return Ops<double>::max(a, dmul_kept(b, c));
+#else
   return Ops<double>::max(a, b * c);
+#endif
 }
 #endif
 
@@ -149,7 +162,7 @@ __device__ __forceinline__ bool bad_density(double r) {
 #ifdef E2D_FP64_NATIVE
   return !(r > 0.0) || !isfinite(r);
 #else
-  const long long b = __double_as_longlong(r);
+  const long long b = (long long)emul::bits(r);
   return b <= 0 || b >= 0x7ff0000000000000ll;  // -0, negative, +0, or +inf / NaN
 #endif
 }
@@ -191,6 +204,46 @@ __device__ __forceinline__ Real cell_invdt(const Hydro<Real>& h, const Real u[4]
 // dcen >= 0, dlim = 0 if dlft*drgt <= 0 else min(|dlft|,|drgt|), and the
 // slope dsgn*min(dlim,|dcen|).  st is 1 or 2; the products by st, 0.5 and
 // dsgn are exact scalings and sign flips.
+// dlim = (dlft*drgt <= 0) ? 0 : slop, slop = min(|dlft|, |drgt|).
+#ifndef E2D_LIMITER_SIGN
+#define E2D_LIMITER_SIGN 0
+#endif
+template <typename Real>
+__device__ __forceinline__ Real limiter_dlim(Real dlft, Real drgt, Real slop) {
+  return Ops<Real>::le0(dlft * drgt) ? Real(0.0) : slop;
+}
+#if !defined(E2D_FP64_NATIVE) && E2D_LIMITER_SIGN
+// For double, the product's sign is decided on the integer pipe when that is
+// exact: finite operands of opposite signs give a product <= 0 (-0 on
+// underflow); a zero operand makes slop +0, the result either way; normal
+// operands of the same sign whose biased exponents sum to at least 972 give
+// |dlft*drgt| >= 2^-1074, a positive product.  The rest (subnormal or tiny
+// same-sign pairs, infinities, NaN) form the IEEE product.
+template <>
+__device__ __forceinline__ double limiter_dlim<double>(double a, double b, double slop) {
+  const int ha = (int)(emul::bits(a) >> 32), hb = (int)(emul::bits(b) >> 32);
+  const unsigned ea = ((unsigned)ha >> 20) & 0x7ffu, eb = ((unsigned)hb >> 20) & 0x7ffu;
+  const bool zero = emul::bits(slop) == 0;
+  const bool opp = (ha ^ hb) < 0;
+  const bool fast = max(ea, eb) < 2047u && (opp || zero || (min(ea, eb) >= 1u && ea + eb >= 972u));
+  double r = (opp || zero) ? 0.0 : slop;
+#if E2D_LIMITER_SIGN == 2
+  if (__any_sync(__activemask(), !fast)) {
+    if (!fast) r = Ops<double>::le0(a * b) ? 0.0 : slop;
+  }
+#elif E2D_LIMITER_SIGN == 3
+  if (!fast) r = Ops<double>::le0(dmul_kept(a, b)) ? 0.0 : slop;
+#elif E2D_LIMITER_SIGN == 4
+  if (__any_sync(__activemask(), !fast)) {
+    if (!fast) r = Ops<double>::le0(dmul_kept(a, b)) ? 0.0 : slop;
+  }
+#else
+  if (!fast) r = Ops<double>::le0(a * b) ? 0.0 : slop;
+#endif
+  return r;
+}
+#endif
+
 template <typename Real>
 __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm) {
   using O = Ops<Real>;
@@ -199,7 +252,7 @@ __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm) {
   const Real drgt = mc ? O::twice(dr) : dr;
   const Real dcen = O::half(qp - qm);
   const Real slop = O::min(rabs(dlft), rabs(drgt));
-  const Real dlim = O::le0(dlft * drgt) ? Real(0.0) : slop;
+  const Real dlim = limiter_dlim(dlft, drgt, slop);
   return O::neg_if(O::min(dlim, rabs(dcen)), !O::ge0(dcen));
 }
 
@@ -323,6 +376,9 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
 }
 
 // riemann_2d_hllc, serial_ref/m_utils.f90:534-644 (rcsum, unused there, is not formed).
+#ifndef E2D_HLLC_ONESTAR
+#define E2D_HLLC_ONESTAR 0
+#endif
 template <typename Real>
 __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real qleft[4],
                                              const Real qright[4], Real flux[4]) {
@@ -353,6 +409,22 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real ustar = O::div(((rcr * ur) + (rcl * ul)) + (ptotl - ptotr), rcr + rcl);
   const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
   Real ro, uo, ptoto, etoto;
+#if E2D_HLLC_ONESTAR
+  // The side first (SL > 0: left state; ustar > 0: left star; SR > 0: right
+  // star; else right state), then one star state from its values.
+  const bool slpos = O::gt0(SL), uspos = O::gt0(ustar);
+  const bool lside = slpos || uspos;
+  const Real SK = lside ? SL : SR, rK = lside ? rl : rr, uK = lside ? ul : ur;
+  const Real eK = lside ? etotl : etotr, pK = lside ? ptotl : ptotr;
+  if (!slpos && (uspos || O::gt0(SR))) {
+    const Real dS = SK - uK, den = SK - ustar;
+    ro = O::div(rK * dS, den);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div((((dS * eK) - (pK * uK)) + (ptotstar * ustar)), den);
+  } else {
+    ro = rK; uo = uK; ptoto = pK; etoto = eK;
+  }
+#else
   if (O::gt0(SL)) {
     ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
   } else if (O::gt0(ustar)) {
@@ -366,6 +438,7 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   } else {
     ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
   }
+#endif
   flux[ID] = ro * uo;
   flux[IU] = ((ro * uo) * uo) + ptoto;
   flux[IP] = (etoto + ptoto) * uo;
