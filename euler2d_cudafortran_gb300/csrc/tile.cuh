@@ -127,8 +127,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   }
   __syncthreads();
 
-  // ---- Riemann fluxes of all faces of the tile, claimed 32 at a time per warp
-  constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1), NF = NXF + NYF;
+  // ---- Riemann fluxes of all faces of the tile, claimed 32 at a time per
+  // warp.  The y faces start on a 32-face boundary, so no warp holds faces of
+  // both directions: the two inlined solvers would both be issued for it
+  // (every FP64 instruction a warp issues costs its FP64 pipe slots,
+  // predicated or not).
+  constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1);
+  constexpr int Y0 = (NXF + 31) / 32 * 32, NF = Y0 + NYF;
   const int lane = tid & 31;
   while (true) {
     int chunk = 0;
@@ -154,8 +159,8 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
 #pragma unroll
         for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = flux[v] * dtdx;
       }
-    } else if (k < NF) {
-      const int kk = k - NXF;
+    } else if (k >= Y0 && k < NF) {
+      const int kk = k - Y0;
       const int c = kk % TX, g = kk / TX;  // between ring cells (c, g-1) and (c, g)
       if (i0 + c <= h.nx + 1 && j0 + g <= h.ny + 2) {
         const int kl = g * RX + (c + 1), kr = kl + RX;
