@@ -50,6 +50,11 @@ struct e2d_run {
   void* u = nullptr;
   void* u2 = nullptr;
   void* work[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // implementationVersion 0: primitive variables beside u (qprim[0]) and u2
+  // (qprim[1]), written by each fused step of e2d_advance / e2d_time_steps for
+  // the next one; refreshed from u and u2 at the start of every such call.
+  // Null when they could not be allocated (the step then converts its box).
+  void* qprim[2] = {nullptr, nullptr};
   Ctl* ctl = nullptr;
   void* dt_log = nullptr;  // device
   int dt_log_cap = 0;
@@ -100,7 +105,7 @@ int use_device(const e2d_run* r) {
 // from_slot: dt comes from the running maximum; otherwise dt_value.
 template <typename Real>
 void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, int wr, int log_index,
-                  bool boundaries_done) {
+                  bool boundaries_done, bool use_q = false) {
   const Hydro<Real>& h = hydro<Real>(r);
   const bool even = (nStep % 2) == 0;
   Field<Real> in = field<Real>(r, even ? r->u : r->u2);
@@ -116,11 +121,14 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
   cudaStream_t s = r->stream;
   if (!boundaries_done) launch_boundaries<Real>(h, in, s);
   switch (r->p.implementation_version) {
-    case 0:
+    case 0: {
       // In the advance path the ghost cells of `out` are written by the
-      // update epilogue (what make_boundaries does at the next step).
-      launch_fused<Real>(h, r->plan, even ? 0 : 1, in, out, sd, r->ctl, from_slot, s);
+      // update epilogue (what make_boundaries does at the next step), and
+      // with use_q the primitives of `out` beside it.
+      const Field<Real> qout = field<Real>(r, r->qprim[even ? 1 : 0]);
+      launch_fused<Real>(h, r->plan, even ? 0 : 1, in, out, sd, r->ctl, from_slot, s, use_q ? &qout : nullptr);
       break;
+    }
     case 1: {
       Field<Real> q = field<Real>(r, r->work[0]);
       launch_prim<Real>(h, in, q, s);
@@ -142,19 +150,34 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
 
 // The device work of e2d_advance: compute_dt on the state of nStep0, ghost
 // fill, then nsteps steps with device-resident dt.
+// implementationVersion 0 with primitive arrays: the primitives of the state
+// of nStep0 (after its ghost fill) and of the other buffer (whose corners no
+// step writes) are formed once; from then on each step writes those of its
+// output.  Returns whether the steps may read them.
+template <typename Real>
+bool refresh_prims(e2d_run* r, int nStep0) {
+  if (r->p.implementation_version != 0 || !r->qprim[0]) return false;
+  const Hydro<Real>& h = hydro<Real>(r);
+  const int b = nStep0 % 2;
+  launch_prim<Real>(h, field<Real>(r, b ? r->u2 : r->u), field<Real>(r, r->qprim[b]), r->stream);
+  launch_prim<Real>(h, field<Real>(r, b ? r->u : r->u2), field<Real>(r, r->qprim[b ^ 1]), r->stream);
+  return true;
+}
+
 template <typename Real>
 void enqueue_advance(e2d_run* r, int nStep0, int nsteps, int slot0, bool seed) {
   const Hydro<Real>& h = hydro<Real>(r);
   Field<Real> cur = field<Real>(r, (nStep0 % 2 == 0) ? r->u : r->u2);
   if (seed) launch_dt_reduce<Real>(h, cur, r->ctl, slot0, r->stream);
   launch_boundaries<Real>(h, cur, r->stream);
+  const bool use_q = refresh_prims<Real>(r, nStep0);
   for (int k = 0; k < nsteps; ++k) {
     const int rd = slot0 ^ (k & 1);
     // implementationVersion 0 fills the ghosts of its output itself; the
     // stored variants run make_boundaries at the start of every step as the
     // reference does (serial_ref/m_run.f90:224).
     const bool bdone = (r->p.implementation_version == 0) || k == 0;
-    enqueue_step<Real>(r, nStep0 + k, Real(0), true, rd, rd ^ 1, k, bdone);
+    enqueue_step<Real>(r, nStep0 + k, Real(0), true, rd, rd ^ 1, k, bdone, use_q);
   }
 }
 
@@ -267,10 +290,20 @@ int e2d_create(const e2d_params* p, e2d_run** out) {
   for (int k = 0; k < nwork; ++k) cudaMemsetAsync(r->work[k], 0, sb, r->stream);
   cudaMemsetAsync(r->ctl, 0, sizeof(Ctl), r->stream);
   if (p->implementation_version == 0) {
-    if (p->precision == 8)
-      r->plan = fused_plan_create<double>(r->hd, field<double>(r, r->u), field<double>(r, r->u2));
-    else
-      r->plan = fused_plan_create<float>(r->hf, field<float>(r, r->u), field<float>(r, r->u2));
+    if (cudaMalloc(&r->qprim[0], sb) != cudaSuccess || cudaMalloc(&r->qprim[1], sb) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(r->qprim[0]);
+      r->qprim[0] = r->qprim[1] = nullptr;
+    }
+    if (p->precision == 8) {
+      const Field<double> q0 = field<double>(r, r->qprim[0]), q1 = field<double>(r, r->qprim[1]);
+      r->plan = fused_plan_create<double>(r->hd, field<double>(r, r->u), field<double>(r, r->u2),
+                                          r->qprim[0] ? &q0 : nullptr, r->qprim[0] ? &q1 : nullptr);
+    } else {
+      const Field<float> q0 = field<float>(r, r->qprim[0]), q1 = field<float>(r, r->qprim[1]);
+      r->plan = fused_plan_create<float>(r->hf, field<float>(r, r->u), field<float>(r, r->u2),
+                                         r->qprim[0] ? &q0 : nullptr, r->qprim[0] ? &q1 : nullptr);
+    }
     if (!r->plan) return cleanup(E2D_ERR_CUDA, "TMA descriptor / kernel attribute setup failed");
   }
   cudaError_t e = cudaStreamSynchronize(r->stream);
@@ -289,6 +322,7 @@ int e2d_destroy(e2d_run* r) {
   cudaFree(r->u);
   cudaFree(r->u2);
   for (void* w : r->work) cudaFree(w);
+  for (void* q : r->qprim) cudaFree(q);
   cudaFree(r->ctl);
   cudaFree(r->dt_log);
   if (r->ev0) cudaEventDestroy(r->ev0);
@@ -535,20 +569,23 @@ int e2d_time_steps(e2d_run* r, int nStep0, int nsteps, float* ms) {
   const int slot0 = r->cur_slot;
   const bool seed = !r->folded[nStep0 % 2];
   const bool v0 = r->p.implementation_version == 0;
+  bool use_q = false;
   if (r->es == 8) {
     Field<double> cur = field<double>(r, (nStep0 % 2 == 0) ? r->u : r->u2);
     if (seed) launch_dt_reduce<double>(r->hd, cur, r->ctl, slot0, r->stream);
     launch_boundaries<double>(r->hd, cur, r->stream);
+    use_q = refresh_prims<double>(r, nStep0);
   } else {
     Field<float> cur = field<float>(r, (nStep0 % 2 == 0) ? r->u : r->u2);
     if (seed) launch_dt_reduce<float>(r->hf, cur, r->ctl, slot0, r->stream);
     launch_boundaries<float>(r->hf, cur, r->stream);
+    use_q = refresh_prims<float>(r, nStep0);
   }
   cudaEventRecord(ev[0], r->stream);
   for (int k = 0; k < nsteps; ++k) {
     const int rd = slot0 ^ (k & 1);
-    if (r->es == 8) enqueue_step<double>(r, nStep0 + k, 0.0, true, rd, rd ^ 1, k, v0 || k == 0);
-    else enqueue_step<float>(r, nStep0 + k, 0.0f, true, rd, rd ^ 1, k, v0 || k == 0);
+    if (r->es == 8) enqueue_step<double>(r, nStep0 + k, 0.0, true, rd, rd ^ 1, k, v0 || k == 0, use_q);
+    else enqueue_step<float>(r, nStep0 + k, 0.0f, true, rd, rd ^ 1, k, v0 || k == 0, use_q);
     cudaEventRecord(ev[k + 1], r->stream);
   }
   cudaError_t e = cudaStreamSynchronize(r->stream);

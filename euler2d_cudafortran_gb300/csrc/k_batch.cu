@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(C::NT, MINB)
       sq[k] = (gi < sh.isize && gj < sh.jsize) ? in.at(v, gj, gi) : Real(0);
     }
     __syncthreads();
-    Real m = tile_compute<Real, C, SQ>(sh, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2], true, wr >= 0,
-                                   &ctls[id].health);
+    Real m = tile_compute<Real, C, SQ>(sh, base, face_counter, red, i0, j0, in, out, out, sdt[1], sdt[2], true,
+                                       wr >= 0, &ctls[id].health);
     if (tid == 0) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];

@@ -24,7 +24,9 @@
 namespace e2d {
 
 struct FusedPlan {
-  CUtensorMap tm[2];  // [0]: u, [1]: u2
+  CUtensorMap tm[2];   // [0]: u, [1]: u2
+  CUtensorMap tmq[2];  // primitives beside u and u2 (when has_q)
+  bool has_q = false;
 };
 
 namespace {
@@ -43,11 +45,13 @@ template <typename Real> struct FusedTile;
 template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, 256>; };
 template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 
-// SQ: dx == dy (the shared face source term of tile_compute).
-template <typename Real, bool SQ>
+// SQ: dx == dy (the shared face source term of tile_compute).  QIN: tm_in
+// maps the primitives of the input state, and the primitives of the output
+// go to qout (tile_compute).
+template <typename Real, bool SQ, bool QIN>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
-            StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
+            Field<Real> qout, StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
   using C = typename FusedTile<Real>::C;
   extern __shared__ unsigned char smem_raw[];
   Real* base = reinterpret_cast<Real*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -92,8 +96,8 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     return;
   }
   const bool want_dt = sd.wr_slot >= 0;
-  Real m = tile_compute<Real, C, SQ>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2],
-                                     fill_ghosts != 0, want_dt, &ctl->health);
+  Real m = tile_compute<Real, C, SQ, QIN>(h, base, face_counter, red, i0, j0, in, out, qout, sdt[1], sdt[2],
+                                          fill_ghosts != 0, want_dt, &ctl->health);
   if (tid == 0) {
     if (blockIdx.x == 0 && blockIdx.y == 0) {
       if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
@@ -120,10 +124,12 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
 // and sources are no longer read then), so the load lands while the update
 // phase runs; the primitives phase of the next tile reads it from there.
 // One mbarrier, one phase per load; every wait is bounded.
-template <typename Real, bool SQ>
+// With QIN the next box goes straight to the primitives region, which the
+// update phase no longer reads.
+template <typename Real, bool SQ, bool QIN>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
-                       StepDt<Real> sd, Ctl* ctl, int fill_ghosts, int ntx, int ntiles) {
+                       Field<Real> qout, StepDt<Real> sd, Ctl* ctl, int fill_ghosts, int ntx, int ntiles) {
   using C = typename FusedTile<Real>::C;
   static_assert(8ull * C::RY * C::RX >= 4ull * C::BYs * C::BXs, "the next box fits in the slope region");
   static_assert((C::d_off * sizeof(Real)) % 128 == 0, "TMA destination alignment of the slope region");
@@ -134,7 +140,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
   int* face_counter = reinterpret_cast<int*>(tail + 8);
   Real* red = reinterpret_cast<Real*>(tail + 16);
   Real* sdt = red + 32;
-  Real* dreg = base + C::d_off;
+  Real* dreg = QIN ? base + C::q_off : base + C::d_off;
   const int tid = threadIdx.x;
   const uint32_t bar_a = smem_u32(bar);
   auto issue = [&](int t, Real* dst) {  // thread 0: the box of tile t into dst
@@ -175,8 +181,9 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     auto prefetch = [&]() {
       if (tid == 0 && next < ntiles) issue(next, dreg);
     };
-    const Real m = tile_compute<Real, C, SQ>(h, base, face_counter, red, i0, j0, in, out, sdt[1], sdt[2],
-                                         fill_ghosts != 0, want_dt, &ctl->health, first ? nullptr : dreg, prefetch);
+    const Real m = tile_compute<Real, C, SQ, QIN>(h, base, face_counter, red, i0, j0, in, out, qout, sdt[1],
+                                                  sdt[2], fill_ghosts != 0, want_dt, &ctl->health,
+                                                  (QIN || first) ? nullptr : dreg, prefetch);
     if (tid == 0) {
       mmax = Ops<Real>::max(mmax, m);
       *face_counter = 0;
@@ -203,7 +210,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 // Resident CTAs per SM x SMs of the current device (the persistent grid).
-template <typename Real, bool SQ>
+template <typename Real, bool SQ, bool QIN>
 int persistent_grid() {
   static int grid[64] = {0};
   int dev = 0;
@@ -213,7 +220,7 @@ int persistent_grid() {
     using C = typename FusedTile<Real>::C;
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real, SQ>, C::NT, C::bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real, SQ, QIN>, C::NT, C::bytes);
     grid[dev] = std::max(1, sms * std::max(1, per_sm));
   }
   return grid[dev];
@@ -221,54 +228,60 @@ int persistent_grid() {
 
 // Dynamic shared memory of the tile, and the largest shared-memory carveout
 // so that as many CTAs as the launch bounds ask for fit on an SM.
-template <typename Real, bool SQ>
+template <typename Real, bool SQ, bool QIN>
 bool set_fused_attributes_sq() {
   using C = typename FusedTile<Real>::C;
-  bool ok = cudaFuncSetAttribute(k_fused<Real, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
-                cudaSuccess &&
-            cudaFuncSetAttribute(k_fused<Real, SQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
+  bool ok = cudaFuncSetAttribute(k_fused<Real, SQ, QIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)C::bytes) == cudaSuccess &&
+            cudaFuncSetAttribute(k_fused<Real, SQ, QIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
   if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT)
     ok = ok &&
-         cudaFuncSetAttribute(k_fused_persistent<Real, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+         cudaFuncSetAttribute(k_fused_persistent<Real, SQ, QIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)C::bytes) == cudaSuccess &&
-         cudaFuncSetAttribute(k_fused_persistent<Real, SQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
+         cudaFuncSetAttribute(k_fused_persistent<Real, SQ, QIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
                               (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
-         persistent_grid<Real, SQ>() > 0;  // sized here, outside any stream capture
+         persistent_grid<Real, SQ, QIN>() > 0;  // sized here, outside any stream capture
   return ok;
 }
 
 template <typename Real>
 bool set_fused_attributes() {
-  return set_fused_attributes_sq<Real, false>() && set_fused_attributes_sq<Real, true>();
+  return set_fused_attributes_sq<Real, false, false>() && set_fused_attributes_sq<Real, true, false>() &&
+         set_fused_attributes_sq<Real, false, true>() && set_fused_attributes_sq<Real, true, true>();
 }
 
-template <typename Real, bool SQ>
-void launch_fused_sq(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out, StepDt<Real> sd,
-                     Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+template <typename Real, bool SQ, bool QIN>
+void launch_fused_sq(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out,
+                     Field<Real> qout, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
   using C = typename FusedTile<Real>::C;
   const int ntx = (h.nx + C::TX - 1) / C::TX, nty = (h.ny + C::TY - 1) / C::TY;
   if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT) {
-    const int grid = std::min(ntx * nty, persistent_grid<Real, SQ>());
-    k_fused_persistent<Real, SQ><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0, ntx,
-                                                               ntx * nty);
+    const int grid = std::min(ntx * nty, persistent_grid<Real, SQ, QIN>());
+    k_fused_persistent<Real, SQ, QIN><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, qout, sd, ctl,
+                                                                    fill_ghosts ? 1 : 0, ntx, ntx * nty);
   } else {
-    k_fused<Real, SQ><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, fill_ghosts ? 1 : 0);
+    k_fused<Real, SQ, QIN><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, qout, sd, ctl,
+                                                                   fill_ghosts ? 1 : 0);
   }
 }
 
 // dx == dy (a square domain of square cells, every benchmark grid) takes the
-// instantiation that forms each cell's face source term once.
+// instantiation that forms each cell's face source term once.  qout set: tm
+// maps the input's primitives (QIN).
 template <typename Real>
-void launch_fused_tm(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out, StepDt<Real> sd,
-                     Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+void launch_fused_tm(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out,
+                     const Field<Real>* qout, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+  const Field<Real> qo = qout ? *qout : out;
 #if E2D_SQ_TRACE
   if (h.dx == h.dy) {
-    launch_fused_sq<Real, true>(tm, h, in, out, sd, ctl, fill_ghosts, s);
+    if (qout) launch_fused_sq<Real, true, true>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
+    else launch_fused_sq<Real, true, false>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
     return;
   }
 #endif
-  launch_fused_sq<Real, false>(tm, h, in, out, sd, ctl, fill_ghosts, s);
+  if (qout) launch_fused_sq<Real, false, true>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
+  else launch_fused_sq<Real, false, false>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
 }
 
 EncodeTiledFn get_encode_fn() {
@@ -303,7 +316,8 @@ bool encode_state_map(CUtensorMap* tm, const Hydro<Real>& h, Field<Real> f) {
 }  // namespace
 
 template <typename Real>
-FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2) {
+FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2, const Field<Real>* q,
+                             const Field<Real>* q2) {
   using C = typename FusedTile<Real>::C;
   static_assert(C::BXs * sizeof(Real) % 16 == 0, "TMA inner box must be a multiple of 16 bytes");
   static_assert((C::TX * sizeof(Real)) % 16 == 0, "tile x origin must stay 16-byte aligned");
@@ -311,6 +325,13 @@ FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2
   if (!encode_state_map<Real>(&p->tm[0], h, u) || !encode_state_map<Real>(&p->tm[1], h, u2)) {
     delete p;
     return nullptr;
+  }
+  if (q && q2) {
+    if (!encode_state_map<Real>(&p->tmq[0], h, *q) || !encode_state_map<Real>(&p->tmq[1], h, *q2)) {
+      delete p;
+      return nullptr;
+    }
+    p->has_q = true;
   }
   if (!set_fused_attributes<Real>()) {
     cudaGetLastError();
@@ -324,8 +345,11 @@ void fused_plan_destroy(FusedPlan* p) { delete p; }
 
 template <typename Real>
 void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in, Field<Real> out,
-                  StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
-  launch_fused_tm<Real>(plan->tm[in_is_u2 ? 1 : 0], h, in, out, sd, ctl, fill_ghosts, s);
+                  StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s, const Field<Real>* qout) {
+  if (qout && plan->has_q)
+    launch_fused_tm<Real>(plan->tmq[in_is_u2 ? 1 : 0], h, in, out, qout, sd, ctl, fill_ghosts, s);
+  else
+    launch_fused_tm<Real>(plan->tm[in_is_u2 ? 1 : 0], h, in, out, nullptr, sd, ctl, fill_ghosts, s);
 }
 
 template <typename Real>
@@ -342,7 +366,8 @@ bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out) {
 template <typename Real>
 void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in, Field<Real> out, StepDt<Real> sd,
                       Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
-  launch_fused_tm<Real>(*reinterpret_cast<const CUtensorMap*>(map.bytes), h, in, out, sd, ctl, fill_ghosts, s);
+  launch_fused_tm<Real>(*reinterpret_cast<const CUtensorMap*>(map.bytes), h, in, out, nullptr, sd, ctl, fill_ghosts,
+                        s);
 }
 
 template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*);
@@ -351,11 +376,13 @@ template void launch_fused_map<double>(const Hydro<double>&, const StateMap&, Fi
                                        StepDt<double>, Ctl*, bool, cudaStream_t);
 template void launch_fused_map<float>(const Hydro<float>&, const StateMap&, Field<float>, Field<float>,
                                       StepDt<float>, Ctl*, bool, cudaStream_t);
-template FusedPlan* fused_plan_create<double>(const Hydro<double>&, Field<double>, Field<double>);
-template FusedPlan* fused_plan_create<float>(const Hydro<float>&, Field<float>, Field<float>);
+template FusedPlan* fused_plan_create<double>(const Hydro<double>&, Field<double>, Field<double>,
+                                              const Field<double>*, const Field<double>*);
+template FusedPlan* fused_plan_create<float>(const Hydro<float>&, Field<float>, Field<float>, const Field<float>*,
+                                             const Field<float>*);
 template void launch_fused<double>(const Hydro<double>&, FusedPlan*, int, Field<double>, Field<double>,
-                                   StepDt<double>, Ctl*, bool, cudaStream_t);
+                                   StepDt<double>, Ctl*, bool, cudaStream_t, const Field<double>*);
 template void launch_fused<float>(const Hydro<float>&, FusedPlan*, int, Field<float>, Field<float>,
-                                  StepDt<float>, Ctl*, bool, cudaStream_t);
+                                  StepDt<float>, Ctl*, bool, cudaStream_t, const Field<float>*);
 
 }  // namespace e2d

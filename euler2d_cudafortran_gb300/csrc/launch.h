@@ -62,13 +62,19 @@ template <typename Real> void launch_flux_update_v1(const Hydro<Real>& h, Field<
                                                     Field<Real> out, StepDt<Real> sd, Ctl* ctl, cudaStream_t s);
 
 // ---- k_fused.cu ---- implementationVersion 0: one fused kernel per step.
-// Builds (once per state buffer) the TMA descriptor of a state.
+// Builds (once per state buffer) the TMA descriptor of a state, and of the
+// primitive-variable arrays q, q2 kept beside u, u2 when they are given.
 struct FusedPlan;
-template <typename Real> FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2);
+template <typename Real> FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2,
+                                                      const Field<Real>* q = nullptr,
+                                                      const Field<Real>* q2 = nullptr);
 void fused_plan_destroy(FusedPlan* p);
+// qout set (and the plan has q arrays): the step reads the primitives of its
+// input from the q array beside it -- they must be current, ghosts and
+// corners included -- and writes those of its output to *qout.
 template <typename Real> void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in,
                                            Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
-                                           cudaStream_t s);
+                                           cudaStream_t s, const Field<Real>* qout = nullptr);
 // A TMA descriptor for any pitched state (used for states outside a run's u/u2).
 struct StateMap { alignas(64) unsigned char bytes[128]; };
 template <typename Real> bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out);

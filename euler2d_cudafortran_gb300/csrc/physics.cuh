@@ -187,16 +187,23 @@ __device__ __forceinline__ Real sound_speed(const Hydro<Real>& h, const Real q[4
   return O::sqrt(O::div(h.gamma0 * q[IP], q[ID]));
 }
 
-// The compute_dt term of one cell, serial_ref/m_run.f90:278-281.
+// The compute_dt term of one cell, serial_ref/m_run.f90:278-281, from the
+// cell's primitive variables q.
 template <typename Real>
-__device__ __forceinline__ Real cell_invdt(const Hydro<Real>& h, const Real u[4]) {
+__device__ __forceinline__ Real cell_invdt_q(const Hydro<Real>& h, const Real q[4]) {
   using O = Ops<Real>;
-  Real q[4];
-  primitives(h, u, q);
   const Real c = sound_speed(h, q);
   const Real vx = c + rabs(q[IU]);
   const Real vy = c + rabs(q[IV]);
   return O::div(vx, h.dx) + O::div(vy, h.dy);
+}
+
+// The same from the conservative variables u.
+template <typename Real>
+__device__ __forceinline__ Real cell_invdt(const Hydro<Real>& h, const Real u[4]) {
+  Real q[4];
+  primitives(h, u, q);
+  return cell_invdt_q(h, q);
 }
 
 // One direction of slope_unsplit_hydro_2d, serial_ref/m_utils.f90:300-312:

@@ -70,11 +70,15 @@ struct NoHook {
 // SQ (only when dx == dy, so that dtdx == dtdy bit for bit): the source term
 // of a face state, (s*dtdx)*0.5, is the same for the four faces of a cell;
 // the ring pass forms it once and stores it in place of s.
-template <typename Real, class C, bool SQ = false, class Hook = NoHook>
+// QIN: the box holds primitive variables already (the previous step wrote
+// them beside its state); the update then writes the primitives of the new
+// state, and of its ghost cells, to qout.  The primitives of a state are a
+// function of its conservative values, so this changes no result.
+template <typename Real, class C, bool SQ = false, bool QIN = false, class Hook = NoHook>
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
                                              int i0, int j0, const Field<Real>& in, const Field<Real>& out,
-                                             Real dtdx, Real dtdy, bool fill_ghosts, bool want_dt,
-                                             unsigned* health, const Real* box_src = nullptr,
+                                             const Field<Real>& qout, Real dtdx, Real dtdy, bool fill_ghosts,
+                                             bool want_dt, unsigned* health, const Real* box_src = nullptr,
                                              Hook after_faces = Hook()) {
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, BXs = C::BXs, BYs = C::BYs, RX = C::RX, RY = C::RY;
   Real* sq = base + C::q_off;
@@ -86,16 +90,18 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
 
   // ---- primitives of the whole box (computePrimitives), in place unless
   // the box was loaded elsewhere
-  const Real* src = box_src ? box_src : sq;
-  for (int k = tid; k < BXs * BYs; k += NT) {
-    Real u[4], q[4];
+  if constexpr (!QIN) {
+    const Real* src = box_src ? box_src : sq;
+    for (int k = tid; k < BXs * BYs; k += NT) {
+      Real u[4], q[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) u[v] = src[v * BXs * BYs + k];
-    primitives(h, u, q);
+      for (int v = 0; v < 4; ++v) u[v] = src[v * BXs * BYs + k];
+      primitives(h, u, q);
 #pragma unroll
-    for (int v = 0; v < 4; ++v) sq[v * BXs * BYs + k] = q[v];
+      for (int v = 0; v < 4; ++v) sq[v * BXs * BYs + k] = q[v];
+    }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- slopes and trace source terms of the ring cells (-1..TX, -1..TY)
   auto Q = [&](int v, int y, int x) -> Real { return sq[(v * BYs + y) * BXs + x]; };
@@ -189,7 +195,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     const int c = k % TX, r = k / TX;
     const int i = i0 + c, j = j0 + r;
     if (i > h.nx + 1 || j > h.ny + 1) continue;
-    Real un[4];
+    Real un[4], qn[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       Real flux_tot = sfx[(v * TY + r) * (TX + 1) + c] - sfx[(v * TY + r) * (TX + 1) + c + 1];
@@ -197,6 +203,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       un[v] = in.at(v, j, i) + flux_tot;
       out.at(v, j, i) = un[v];
     }
+    if constexpr (QIN) {
+      primitives(h, un, qn);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) qout.at(v, j, i) = qn[v];
+    }
+    // Ghost copies (reflective walls flip the normal momentum, and so the
+    // normal velocity of the primitives: -m/rho is -(m/rho) exactly).
     if (fill_ghosts) {
       if (i <= 3 || i >= h.nx) {
 #pragma unroll
@@ -205,8 +218,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
           const int type = (e < 2) ? h.bc_xmin : h.bc_xmax;
           if (ghost_source(g, h.nx, type) == i) {
 #pragma unroll
-            for (int v = 0; v < 4; ++v)
+            for (int v = 0; v < 4; ++v) {
               out.at(v, j, g) = Ops<Real>::neg_if(un[v], type == 1 && v == IU);  // reflective: flip u
+              if constexpr (QIN) qout.at(v, j, g) = Ops<Real>::neg_if(qn[v], type == 1 && v == IU);
+            }
           }
         }
       }
@@ -217,14 +232,19 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
           const int type = (e < 2) ? h.bc_ymin : h.bc_ymax;
           if (ghost_source(g, h.ny, type) == j) {
 #pragma unroll
-            for (int v = 0; v < 4; ++v)
+            for (int v = 0; v < 4; ++v) {
               out.at(v, g, i) = Ops<Real>::neg_if(un[v], type == 1 && v == IV);  // reflective: flip v
+              if constexpr (QIN) qout.at(v, g, i) = Ops<Real>::neg_if(qn[v], type == 1 && v == IV);
+            }
           }
         }
       }
     }
     if (bad_density(un[ID])) atomicOr(health, 2u);
-    if (want_dt && i <= h.isize - 4 && j <= h.jsize - 4) m = Ops<Real>::max(m, cell_invdt(h, un));
+    if (want_dt && i <= h.isize - 4 && j <= h.jsize - 4) {
+      if constexpr (QIN) m = Ops<Real>::max(m, cell_invdt_q(h, qn));
+      else m = Ops<Real>::max(m, cell_invdt(h, un));
+    }
   }
   if (want_dt) {
 #pragma unroll
