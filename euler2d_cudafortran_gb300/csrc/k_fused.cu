@@ -45,13 +45,28 @@ template <typename Real> struct FusedTile;
 template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, 256>; };
 template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 
+#ifndef E2D_PREFETCH_CONS
+#define E2D_PREFETCH_CONS 1
+#endif
+
+// Asks the TMA unit to bring a box of the map into L2 (no completion to wait for).
+__device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* tm, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                   reinterpret_cast<uint64_t>(tm)),
+               "r"(x), "r"(y), "r"(0)
+               : "memory");
+}
+
 // SQ: dx == dy (the shared face source term of tile_compute).  QIN: tm_in
 // maps the primitives of the input state, and the primitives of the output
-// go to qout (tile_compute).
+// go to qout (tile_compute); in FP32 the tile's conservative values, which
+// only the update reads, are prefetched into L2 through tm_cons when the box
+// load is issued (+7 % there; the FP64 step, bound by its FP64 pipe, measured
+// no gain from it).
 template <typename Real, bool SQ, bool QIN>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
-    k_fused(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
-            Field<Real> qout, StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
+    k_fused(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_cons, Hydro<Real> h,
+            Field<Real> in, Field<Real> out, Field<Real> qout, StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
   using C = typename FusedTile<Real>::C;
   extern __shared__ unsigned char smem_raw[];
   Real* base = reinterpret_cast<Real*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -88,6 +103,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
             "r"(smem_u32(base + C::q_off)),
         "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
         : "memory");
+    if (QIN && E2D_PREFETCH_CONS && sizeof(Real) == 4) prefetch_box_l2(&tm_cons, i0 - GW, j0 - GW);
   }
   const Real dt = sdt[0];
   const bool ok = mbar_wait(bar_a, 0, kTmaWaitCycles);
@@ -128,8 +144,9 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
 // update phase no longer reads.
 template <typename Real, bool SQ, bool QIN>
 __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
-    k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, Hydro<Real> h, Field<Real> in, Field<Real> out,
-                       Field<Real> qout, StepDt<Real> sd, Ctl* ctl, int fill_ghosts, int ntx, int ntiles) {
+    k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_cons,
+                       Hydro<Real> h, Field<Real> in, Field<Real> out, Field<Real> qout, StepDt<Real> sd, Ctl* ctl,
+                       int fill_ghosts, int ntx, int ntiles) {
   using C = typename FusedTile<Real>::C;
   static_assert(8ull * C::RY * C::RX >= 4ull * C::BYs * C::BXs, "the next box fits in the slope region");
   static_assert((C::d_off * sizeof(Real)) % 128 == 0, "TMA destination alignment of the slope region");
@@ -153,6 +170,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
             "r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
         : "memory");
+    if (QIN && E2D_PREFETCH_CONS && sizeof(Real) == 4) prefetch_box_l2(&tm_cons, i0 - GW, j0 - GW);
   };
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
@@ -252,36 +270,38 @@ bool set_fused_attributes() {
 }
 
 template <typename Real, bool SQ, bool QIN>
-void launch_fused_sq(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out,
-                     Field<Real> qout, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+void launch_fused_sq(const CUtensorMap& tm, const CUtensorMap& tmc, const Hydro<Real>& h, Field<Real> in,
+                     Field<Real> out, Field<Real> qout, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
+                     cudaStream_t s) {
   using C = typename FusedTile<Real>::C;
   const int ntx = (h.nx + C::TX - 1) / C::TX, nty = (h.ny + C::TY - 1) / C::TY;
   if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT) {
     const int grid = std::min(ntx * nty, persistent_grid<Real, SQ, QIN>());
-    k_fused_persistent<Real, SQ, QIN><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, qout, sd, ctl,
+    k_fused_persistent<Real, SQ, QIN><<<grid, C::NT, C::bytes, s>>>(tm, tmc, h, in, out, qout, sd, ctl,
                                                                     fill_ghosts ? 1 : 0, ntx, ntx * nty);
   } else {
-    k_fused<Real, SQ, QIN><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, qout, sd, ctl,
+    k_fused<Real, SQ, QIN><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, tmc, h, in, out, qout, sd, ctl,
                                                                    fill_ghosts ? 1 : 0);
   }
 }
 
 // dx == dy (a square domain of square cells, every benchmark grid) takes the
 // instantiation that forms each cell's face source term once.  qout set: tm
-// maps the input's primitives (QIN).
+// maps the input's primitives (QIN) and tmc its conservative values.
 template <typename Real>
-void launch_fused_tm(const CUtensorMap& tm, const Hydro<Real>& h, Field<Real> in, Field<Real> out,
-                     const Field<Real>* qout, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
+void launch_fused_tm(const CUtensorMap& tm, const CUtensorMap& tmc, const Hydro<Real>& h, Field<Real> in,
+                     Field<Real> out, const Field<Real>* qout, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
+                     cudaStream_t s) {
   const Field<Real> qo = qout ? *qout : out;
 #if E2D_SQ_TRACE
   if (h.dx == h.dy) {
-    if (qout) launch_fused_sq<Real, true, true>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
-    else launch_fused_sq<Real, true, false>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
+    if (qout) launch_fused_sq<Real, true, true>(tm, tmc, h, in, out, qo, sd, ctl, fill_ghosts, s);
+    else launch_fused_sq<Real, true, false>(tm, tmc, h, in, out, qo, sd, ctl, fill_ghosts, s);
     return;
   }
 #endif
-  if (qout) launch_fused_sq<Real, false, true>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
-  else launch_fused_sq<Real, false, false>(tm, h, in, out, qo, sd, ctl, fill_ghosts, s);
+  if (qout) launch_fused_sq<Real, false, true>(tm, tmc, h, in, out, qo, sd, ctl, fill_ghosts, s);
+  else launch_fused_sq<Real, false, false>(tm, tmc, h, in, out, qo, sd, ctl, fill_ghosts, s);
 }
 
 EncodeTiledFn get_encode_fn() {
@@ -346,10 +366,11 @@ void fused_plan_destroy(FusedPlan* p) { delete p; }
 template <typename Real>
 void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in, Field<Real> out,
                   StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s, const Field<Real>* qout) {
+  const CUtensorMap& tmc = plan->tm[in_is_u2 ? 1 : 0];
   if (qout && plan->has_q)
-    launch_fused_tm<Real>(plan->tmq[in_is_u2 ? 1 : 0], h, in, out, qout, sd, ctl, fill_ghosts, s);
+    launch_fused_tm<Real>(plan->tmq[in_is_u2 ? 1 : 0], tmc, h, in, out, qout, sd, ctl, fill_ghosts, s);
   else
-    launch_fused_tm<Real>(plan->tm[in_is_u2 ? 1 : 0], h, in, out, nullptr, sd, ctl, fill_ghosts, s);
+    launch_fused_tm<Real>(tmc, tmc, h, in, out, nullptr, sd, ctl, fill_ghosts, s);
 }
 
 template <typename Real>
@@ -366,8 +387,8 @@ bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out) {
 template <typename Real>
 void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in, Field<Real> out, StepDt<Real> sd,
                       Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
-  launch_fused_tm<Real>(*reinterpret_cast<const CUtensorMap*>(map.bytes), h, in, out, nullptr, sd, ctl, fill_ghosts,
-                        s);
+  const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(map.bytes);
+  launch_fused_tm<Real>(tm, tm, h, in, out, nullptr, sd, ctl, fill_ghosts, s);
 }
 
 template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*);
