@@ -17,6 +17,10 @@ namespace adj {
 
 using O = Ops<double>;
 
+#ifndef E2D_REV_ONESTAR
+#define E2D_REV_ONESTAR 1
+#endif
+
 __device__ __forceinline__ bool picks_first_max(double a, double b) { return emul::gt_i(a, b); }  // max(a,b) == a
 __device__ __forceinline__ bool picks_first_min(double a, double b) { return emul::ord(a) < emul::ord(b); }
 
@@ -150,8 +154,8 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
                                                  double flux[4]) {
   // ---- forward recomputation (same operations and branches as riemann_hllc)
   const double rl = O::max(ql[ID], h.smallr), rr = O::max(qr[ID], h.smallr);
-  const double rlsp = rl * h.smallp, rrsp = rr * h.smallp;
-  const double pl = O::max(ql[IP], rlsp), pr = O::max(qr[IP], rrsp);
+  bool pl_raw, pr_raw;  // the pressure floors returned the face pressures
+  const double pl = floor_pick(ql[IP], rl, h.smallp, pl_raw), pr = floor_pick(qr[IP], rr, h.smallp, pr_raw);
   const double ul = ql[IU], ur = qr[IU], vl = ql[IV], vr = qr[IV];
   const double hrl = O::half(rl), hrr = O::half(rr);
   const double etotl = (pl * h.entho) + (((hrl * ul) * ul) + ((hrl * vl) * vl));
@@ -168,6 +172,23 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   const double den = rcr + rcl;
   const double ustar = O::div(((rcr * ur) + (rcl * ul)) + (pl - pr), den);
   const double ptotstar = O::div(((rcr * pl) + (rcl * pr)) + ((rcl * rcr) * (ul - ur)), den);
+#if E2D_REV_ONESTAR
+  // The sampled side K first (SL > 0: left state; ustar > 0: left star;
+  // SR > 0: right star; else right state), then one star state from its
+  // values: a warp whose faces sample both stars issues the arithmetic once.
+  const bool b1 = O::gt0(SL), b2 = !b1 && O::gt0(ustar);
+  const bool star = b2 || (!b1 && O::gt0(SR));
+  const bool lside = b1 || b2;
+  const double SK = lside ? SL : SR, rK = lside ? rl : rr, uK = lside ? ul : ur;
+  const double eK = lside ? etotl : etotr, pK = lside ? pl : pr;
+  double ro = rK, uo = uK, ptoto = pK, etoto = eK, d = 1.0, dS = 0.0;
+  if (star) {
+    dS = SK - uK;
+    d = SK - ustar;
+    ro = O::div(rK * dS, d); uo = ustar; ptoto = ptotstar;
+    etoto = O::div((((dS * eK) - (pK * uK)) + (ptotstar * ustar)), d);
+  }
+#else
   int branch;
   double ro, uo, ptoto, etoto, d = 1.0, nE = 0.0;
   if (O::gt0(SL)) { branch = 1; ro = rl; uo = ul; ptoto = pl; etoto = etotl; }
@@ -180,6 +201,7 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
     ro = O::div(rr * (SR - ur), d); uo = ustar; ptoto = ptotstar;
     nE = (((SR - ur) * etotr) - (pr * ur)) + (ptotstar * ustar); etoto = O::div(nE, d);
   } else { branch = 4; ro = rr; uo = ur; ptoto = pr; etoto = etotr; }
+#endif
   const double fr = ro * uo;
   const bool vleft = O::gt0(fr);
   flux[ID] = fr;
@@ -201,6 +223,27 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   // fr = ro * uo
   double rob = frb * uo;
   uob += frb * ro;
+#if E2D_REV_ONESTAR
+  {
+    double rKb = rob, uKb = uob, pKb = ptotob, eKb = etotob, SKb = 0.0;
+    if (star) {
+      ustarb += uob; ptotstarb += ptotob;
+      const double rq = O::div(rob, d);
+      rKb = rq * dS; SKb = rq * rK; uKb = O::neg_if(rq * rK, true);
+      const double nEb = O::div(etotob, d);
+      const double db = O::neg_if(rq * ro + nEb * etoto, true);
+      SKb += nEb * eK; uKb -= nEb * eK; eKb = nEb * dS;
+      pKb = O::neg_if(nEb * uK, true); uKb -= nEb * pK; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
+      SKb += db; ustarb -= db;
+    }
+    // the side's accumulators are all zero here: route by selection
+    rlb = lside ? rKb : 0.0; rrb = lside ? 0.0 : rKb;
+    ulb = lside ? uKb : 0.0; urb = lside ? 0.0 : uKb;
+    plb = lside ? pKb : 0.0; prb = lside ? 0.0 : pKb;
+    etotlb = lside ? eKb : 0.0; etotrb = lside ? 0.0 : eKb;
+    SLb = lside ? SKb : 0.0; SRb = lside ? 0.0 : SKb;
+  }
+#else
   switch (branch) {
     case 1: rlb += rob; ulb += uob; plb += ptotob; etotlb += etotob; break;
     case 4: rrb += rob; urb += uob; prb += ptotob; etotrb += etotob; break;
@@ -227,6 +270,7 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
       break;
     }
   }
+#endif
   // ptotstar and ustar = num / den
   const double npb = O::div(ptotstarb, den), nub = O::div(ustarb, den);
   double denb = -npb * ptotstar - nub * ustar;
@@ -263,8 +307,8 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   ulb += erl * ul; vlb += erl * vl;
   urb += err * ur; vrb += err * vr;
   // pressure and density floors
-  if (picks_first_max(ql[IP], rlsp)) qlb[IP] += plb; else rlb += plb * h.smallp;
-  if (picks_first_max(qr[IP], rrsp)) qrb[IP] += prb; else rrb += prb * h.smallp;
+  if (pl_raw) qlb[IP] += plb; else rlb += plb * h.smallp;
+  if (pr_raw) qrb[IP] += prb; else rrb += prb * h.smallp;
   if (picks_first_max(ql[ID], h.smallr)) qlb[ID] += rlb;
   if (picks_first_max(qr[ID], h.smallr)) qrb[ID] += rrb;
   qlb[IU] += ulb; qlb[IV] += vlb;

@@ -57,7 +57,9 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   __shared__ double red[2][ANT / 32];
   const int tid = threadIdx.x;
   const int i0 = GW + bx * ATX, j0 = GW + by * ATY;
-  const double dtdx = dt / h.dx, dtdy = dt / h.dy;
+  // (the integer-pipe division: the same bits as dt / dx, without the FP64
+  // instructions every thread would otherwise spend on it)
+  const double dtdx = Ops<double>::div(dt, h.dx), dtdy = Ops<double>::div(dt, h.dy);
   if (ubz.p) {
     for (int k = tid; k < 4 * ATX * ATY; k += ANT) {
       const int v = k / (ATX * ATY), rem = k - v * (ATX * ATY), y = rem / ATX, x = rem - y * ATX;
@@ -190,9 +192,13 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       }
       double qab[4] = {0, 0, 0, 0}, dqab[4] = {0, 0, 0, 0}, sab[4] = {0, 0, 0, 0};
       double qbb[4] = {0, 0, 0, 0}, dqbb[4] = {0, 0, 0, 0}, sbb[4] = {0, 0, 0, 0};
-      double& dtdb = xface ? dtdxb : dtdyb;
+      // (a local accumulator: a reference selecting dtdxb or dtdyb would put
+      // both in local memory)
+      double dtdb = 0.0;
       adj::trace_face_rev<true>(h, qa, dqa, sa, dtd, qlb, qab, dqab, sab, dtdb);
       adj::trace_face_rev<false>(h, qb_, dqb, sb, dtd, qrb, qbb, dqbb, sbb, dtdb);
+      if (xface) dtdxb += dtdb;
+      else dtdyb += dtdb;
       const int ka = ja * ABX + ia;
       const int kb = xface ? ka + 1 : ka + ABX;
 #pragma unroll
@@ -266,7 +272,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       if (rs >= 0) t += sra[(8 + v) * NRING + rs];    // south neighbour's north adjoint
       if (rn >= 0) t += ss[v * NRING + rn];           // north neighbour's south adjoint
       qb[v] = t;
-      any |= t != 0.0;
+      any |= (emul::bits(t) << 1) != 0;  // t != 0, decided on the integer pipe
     }
     if (any) {
       double qf[4];  // the forward primitives, still in the box
@@ -281,7 +287,8 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
         for (int v = 0; v < 4; ++v) ub[v] += UB(v, gi, gj);
       }
 #pragma unroll
-      for (int v = 0; v < 4; ++v) if (ub[v] != 0.0) atomicAdd(&ubn.at(v, gj, gi), ub[v]);
+      for (int v = 0; v < 4; ++v)
+        if ((emul::bits(ub[v]) << 1) != 0) atomicAdd(&ubn.at(v, gj, gi), ub[v]);
     } else if (any) {
       int si = gi, sj = gj, type, flip;
       if (!xin) {
@@ -296,7 +303,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const double g = Ops<double>::neg_if(ub[v], type == 1 && v == flip);
-        if (g != 0.0) atomicAdd(&ubn.at(v, sj, si), g);
+        if ((emul::bits(g) << 1) != 0) atomicAdd(&ubn.at(v, sj, si), g);  // g != 0
       }
     }
   }

@@ -155,6 +155,22 @@ template <> __device__ __forceinline__ double floor_prod<double>(double a, doubl
 }
 #endif
 
+// The same maximum, also telling whether it returned a (the derivative then
+// flows to a, else to b*c).
+__device__ __forceinline__ double floor_pick(double a, double b, double c, bool& first) {
+#if !defined(E2D_FP64_NATIVE) && E2D_PFLOOR_EXP
+  const int ha = (int)(emul::bits(a) >> 32), hb = (int)(emul::bits(b) >> 32), hc = (int)(emul::bits(c) >> 32);
+  if ((unsigned)(ha - 0x00100000) < 0x7fe00000u && (unsigned)hb < 0x7ff00000u && (unsigned)hc < 0x7ff00000u &&
+      (ha >> 20) >= (hb >> 20) + (hc >> 20) - 1021) {
+    first = true;
+    return a;
+  }
+#endif
+  const double bc = b * c;
+  first = Ops<double>::gt(a, bc);
+  return first ? a : bc;
+}
+
 // A new density that is not a positive finite number (the health check of the
 // update; for double decided on the integer pipe).
 __device__ __forceinline__ bool bad_density(float r) { return !(r > 0.0f) || !isfinite(r); }
