@@ -103,6 +103,7 @@ AdjBatch view(const e2d_adjoint_batch* b) {
   B.nprob = b->nprob;
   B.total_tiles = b->rev_tiles;
   B.nparts = b->nparts;
+  B.square = b->square;
   B.dt_log = b->dt_log;
   B.inv_log = b->inv_log;
   B.dtbar_log = b->dtbar_log;

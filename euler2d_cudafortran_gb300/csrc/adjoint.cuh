@@ -128,13 +128,16 @@ __device__ __forceinline__ void trace_sources_rev(const Hydro<double>& h, const 
 }
 
 // trace_face reverse: qfb -> (qb, dqb, sb) and the dt/d adjoint dtdb.
-template <bool PLUS>
+// PRE: sh holds (s*dtd)*0.5 (dx == dy), and sb receives the adjoint of
+// (s*dtd) per unit dtd -- the caller multiplies the cell's sum by dtd once.
+template <bool PLUS, bool PRE = false>
 __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const double q[4], const double dq[4],
-                                               const double s[4], double dtd, const double qfb_in[4],
-                                               double qb[4], double dqb[4], double sb[4], double& dtdb) {
+                                               const double s[4], const double* sh, double dtd,
+                                               const double qfb_in[4], double qb[4], double dqb[4], double sb[4],
+                                               double& dtdb) {
   double qfb[4] = {qfb_in[0], qfb_in[1], qfb_in[2], qfb_in[3]};
   const double a = PLUS ? (q[ID] + O::half(dq[ID])) : (q[ID] - O::half(dq[ID]));
-  const double raw = a + O::half(s[ID] * dtd);
+  const double raw = a + (PRE ? sh[ID] : O::half(s[ID] * dtd));
   // max(smallr, raw) returns raw unless smallr > raw: no gradient through the floor
   if (emul::gt_i(h.smallr, raw)) qfb[ID] = 0.0;
 #pragma unroll
@@ -142,7 +145,7 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
     const double hq = O::half(qfb[v]);
     qb[v] += qfb[v];
     dqb[v] += O::neg_if(hq, !PLUS);
-    sb[v] += dtd * hq;
+    sb[v] += PRE ? hq : dtd * hq;
     dtdb += s[v] * hq;
   }
 }

@@ -28,6 +28,7 @@ struct AdjBatch {
   double* J;
   double* part_v;
   long long* part_i;
+  bool square = false;  // every problem has dx == dy
 };
 
 int batch_step_rev_setup();

@@ -20,15 +20,18 @@ namespace e2d {
 
 namespace {
 
-// Reverse tile: 32 x E2D_REV_TY cells, 128 threads, E2D_REV_MINB CTAs per SM
-// (shared memory and registers must allow that many).
+// Reverse tile: 32 x E2D_REV_TY cells, E2D_REV_NT threads, E2D_REV_MINB CTAs
+// per SM (shared memory and registers must allow that many).
 #ifndef E2D_REV_TY
 #define E2D_REV_TY 7
+#endif
+#ifndef E2D_REV_NT
+#define E2D_REV_NT 128
 #endif
 #ifndef E2D_REV_MINB
 #define E2D_REV_MINB 2
 #endif
-constexpr int ATX = 32, ATY = E2D_REV_TY, ANT = 128;
+constexpr int ATX = 32, ATY = E2D_REV_TY, ANT = E2D_REV_NT;
 constexpr int ABX = ATX + 4, ABY = ATY + 4, ARX = ATX + 2, ARY = ATY + 2;
 constexpr int NBOX = ABX * ABY, NRING = ARX * ARY;
 constexpr int NUB = (ATX + 1) * (ATY + 1);
@@ -39,12 +42,17 @@ constexpr int S_OFF = DQ_OFF + 8 * NRING;       // sources    [4][ARY][ARX]
 constexpr int UB_OFF = S_OFF + 4 * NRING;       // Ubar'      [4][ATY+1][ATX+1], cells (i0-1.., j0-1..)
 constexpr int RA_OFF = UB_OFF + 4 * NUB;        // ring adj.  dqx[4] dqy[4] s[4]: [12][ARY][ARX]
 constexpr int QB_OFF = RA_OFF + 12 * NRING;     // q adjoint  [4][ABY][ABX]
-constexpr int N_SMEM = QB_OFF + 4 * NBOX;
+constexpr int SH_OFF = QB_OFF + 4 * NBOX;       // (s*dtd)/2  [4][ARY][ARX] (dx == dy only)
+constexpr int N_SMEM = SH_OFF + 4 * NRING;
 constexpr size_t SMEM_BYTES = (size_t)N_SMEM * sizeof(double) + 64;
 
 // One 32 x 7 tile (bx, by) of the reverse step; sm is the dynamic shared area.
 // ubz (if set) is the adjoint buffer of the following reverse step: the
 // tile's interior cells of it are zeroed here (nothing reads it now).
+// SQ (dx == dy, so dtdx == dtdy): the face source term (s*dtd)*0.5 is formed
+// once per ring cell, and the source adjoints are summed per unit dtd and
+// scaled once per ring cell.
+template <bool SQ>
 __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
                                               Field<double> ubn, Field<double> ubz, double dt, double* dtbar,
                                               int bx, int by, double* sm) {
@@ -54,6 +62,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   double* sub = sm + UB_OFF;
   double* sra = sm + RA_OFF;
   double* sqb = sm + QB_OFF;
+  double* ssh = sm + SH_OFF;
   __shared__ double red[2][ANT / 32];
   const int tid = threadIdx.x;
   const int i0 = GW + bx * ATX, j0 = GW + by * ATY;
@@ -108,6 +117,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       sdq[v * NRING + k] = dqx[v];
       sdq[(4 + v) * NRING + k] = dqy[v];
       ss[v * NRING + k] = s[v];
+      if constexpr (SQ) ssh[v * NRING + k] = Ops<double>::half(s[v] * dtdx);
     }
   }
   __syncthreads();
@@ -157,16 +167,22 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     if (valid) {
       const double dtd = xface ? dtdx : dtdy;
       const int nrm = xface ? 0 : 4;  // slope block of the face normal
-      double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], ql[4], qr[4];
+      double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], sha[4], shb[4], ql[4], qr[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         qa[v] = Q(v, ja, ia);
         qb_[v] = xface ? Q(v, ja, ia + 1) : Q(v, ja + 1, ia);
         dqa[v] = sdq[(nrm + v) * NRING + a]; dqb[v] = sdq[(nrm + v) * NRING + b];
         sa[v] = ss[v * NRING + a]; sb[v] = ss[v * NRING + b];
+        if constexpr (SQ) { sha[v] = ssh[v * NRING + a]; shb[v] = ssh[v * NRING + b]; }
       }
-      trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
-      trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
+      if constexpr (SQ) {
+        trace_face<double, true, true>(h, qa, dqa, sha, dtd, ql);
+        trace_face<double, false, true>(h, qb_, dqb, shb, dtd, qr);
+      } else {
+        trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
+        trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
+      }
       if (!xface) {
         double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
         t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
@@ -195,8 +211,8 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       // (a local accumulator: a reference selecting dtdxb or dtdyb would put
       // both in local memory)
       double dtdb = 0.0;
-      adj::trace_face_rev<true>(h, qa, dqa, sa, dtd, qlb, qab, dqab, sab, dtdb);
-      adj::trace_face_rev<false>(h, qb_, dqb, sb, dtd, qrb, qbb, dqbb, sbb, dtdb);
+      adj::trace_face_rev<true, SQ>(h, qa, dqa, sa, sha, dtd, qlb, qab, dqab, sab, dtdb);
+      adj::trace_face_rev<false, SQ>(h, qb_, dqb, sb, shb, dtd, qrb, qbb, dqbb, sbb, dtdb);
       if (xface) dtdxb += dtdb;
       else dtdyb += dtdb;
       const int ka = ja * ABX + ia;
@@ -231,6 +247,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       dqx[v] = sdq[v * NRING + k]; dqy[v] = sdq[(4 + v) * NRING + k];
       dqxb[v] = sra[v * NRING + k]; dqyb[v] = sra[(4 + v) * NRING + k];
       sbar[v] = sra[(8 + v) * NRING + k];
+      if constexpr (SQ) sbar[v] = sbar[v] * dtdx;  // summed per unit dtd by the face pass
     }
     adj::trace_sources_rev(h, qc, dqx, dqy, sbar, qcb, dqxb, dqyb);
     const int kc = y * ABX + x;
@@ -322,11 +339,12 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   }
 }
 
+template <bool SQ>
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, Field<double> ubz,
                const double* dt, double* dtbar) {
   extern __shared__ double sm[];
-  step_rev_tile(h, un, ubn1, ubn, ubz, *dt, dtbar, blockIdx.x, blockIdx.y, sm);
+  step_rev_tile<SQ>(h, un, ubn1, ubn, ubz, *dt, dtbar, blockIdx.x, blockIdx.y, sm);
 }
 
 // The 2x2 ghost corners are never written by a step, so a state keeps the
@@ -493,6 +511,7 @@ __device__ __forceinline__ Field<double> afield(const AdjProb& P, int k) {
 
 // Reverse step m of every problem: one CTA per 32 x 7 tile of the flattened
 // tile list (problem p owns tiles [tile_begin, tile_begin + ntx * nty)).
+template <bool SQ>
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_batch_step_rev(const AdjProb* __restrict__ probs, int nprob, const double* dt_log, double* dtbar_log, int un,
                      int ub_in, int ub_out, int ub_zero, int m) {
@@ -514,7 +533,7 @@ __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
   const AdjProb& P = probs[sp];
   const int tile = t - P.tile_begin;
   const long long row = (long long)m * nprob + sp;
-  step_rev_tile(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out),
+  step_rev_tile<SQ>(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out),
                 ub_zero >= 0 ? afield(P, ub_zero) : Field<double>{nullptr, 0, 0}, dt_log[row], dtbar_log + row,
                 tile % P.ntx, tile / P.ntx, sm);
 }
@@ -581,8 +600,10 @@ __global__ void k_batch_extract(const AdjProb* __restrict__ probs, int ub, doubl
 }  // namespace
 
 int step_rev_setup() {
-  return cudaFuncSetAttribute(k_step_rev, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
-                 cudaSuccess
+  return cudaFuncSetAttribute(k_step_rev<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
+                     cudaSuccess &&
+                 cudaFuncSetAttribute(k_step_rev<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)SMEM_BYTES) == cudaSuccess
              ? 0
              : -1;
 }
@@ -590,7 +611,8 @@ int step_rev_setup() {
 void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn1, Field<double> ubn,
                      Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s) {
   dim3 g((h.nx + ATX - 1) / ATX, (h.ny + ATY - 1) / ATY);
-  k_step_rev<<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar);
+  if (h.dx == h.dy) k_step_rev<true><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar);
+  else k_step_rev<false><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar);
 }
 
 void launch_seg_corners(const Hydro<double>& h, double* pool, size_t state_elems, size_t pitch, size_t plane,
@@ -617,8 +639,10 @@ void launch_objective(const Hydro<double>& h, Field<double> u, double xc, double
 }
 
 int batch_step_rev_setup() {
-  return cudaFuncSetAttribute(k_batch_step_rev, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
-                 cudaSuccess
+  return cudaFuncSetAttribute(k_batch_step_rev<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)SMEM_BYTES) == cudaSuccess &&
+                 cudaFuncSetAttribute(k_batch_step_rev<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)SMEM_BYTES) == cudaSuccess
              ? 0
              : -1;
 }
@@ -630,8 +654,12 @@ int rev_tile_shape(int* tx, int* ty) {
 }
 
 void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s) {
-  k_batch_step_rev<<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in, ub_out,
-                                                          ub_zero, m);
+  if (B.square)
+    k_batch_step_rev<true><<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in,
+                                                                  ub_out, ub_zero, m);
+  else
+    k_batch_step_rev<false><<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in,
+                                                                   ub_out, ub_zero, m);
 }
 
 void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s) {
