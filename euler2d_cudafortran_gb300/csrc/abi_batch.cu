@@ -30,6 +30,11 @@ struct e2d_batch {
   size_t pool_elems = 0;
   void* pool_u = nullptr;
   void* pool_u2 = nullptr;
+  // primitives beside pool_u / pool_u2, written by each step for the next and
+  // refreshed at the start of every advance; null when they could not be
+  // allocated (the steps then convert their boxes)
+  void* pool_q = nullptr;
+  void* pool_q2 = nullptr;
   Ctl* ctls = nullptr;
   void* d_probs = nullptr;  // BatchProb<Real>[nprob], work-list order
   void* d_dtlog = nullptr;
@@ -65,6 +70,13 @@ Field<Real> bfield(const e2d_batch* b, int p, int which) {
   return Field<Real>{base + b->off[p], (int)b->pitch[p], (long long)b->plane[p]};
 }
 
+// The primitives kept beside state `which` of problem p (pool_q must be set).
+template <typename Real>
+Field<Real> qfield(const e2d_batch* b, int p, int which) {
+  Real* base = static_cast<Real*>(which ? b->pool_q2 : b->pool_q);
+  return Field<Real>{base + b->off[p], (int)b->pitch[p], (long long)b->plane[p]};
+}
+
 void clear_graphs(e2d_batch* b) {
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   b->graphs.clear();
@@ -89,6 +101,8 @@ int build_worklist(e2d_batch* b) {
     P.h = bh<Real>(b, p);
     P.u = bfield<Real>(b, p, 0).p;
     P.u2 = bfield<Real>(b, p, 1).p;
+    P.q = b->pool_q ? qfield<Real>(b, p, 0).p : nullptr;
+    P.q2 = b->pool_q ? qfield<Real>(b, p, 1).p : nullptr;
     P.pitch = (int)b->pitch[p];
     P.plane = (long long)b->plane[p];
     P.ntx = (b->params[p].nx + tx - 1) / tx;
@@ -116,10 +130,15 @@ int build(e2d_batch* b) { return b->es == 8 ? build_worklist<double>(b) : build_
 
 template <typename Real>
 void enqueue(e2d_batch* b, int nStep0, int nsteps, int slot0, bool seed) {
+  const int b0 = nStep0 % 2;
   for (int p = 0; p < b->nprob; ++p) {
-    Field<Real> cur = bfield<Real>(b, p, nStep0 % 2);
+    Field<Real> cur = bfield<Real>(b, p, b0);
     if (seed) launch_dt_reduce<Real>(bh<Real>(b, p), cur, &b->ctls[p], slot0, b->stream);
     launch_boundaries<Real>(bh<Real>(b, p), cur, b->stream);
+    if (b->pool_q) {  // the primitives of the state, and of the other buffer (whose corners no step writes)
+      launch_prim<Real>(bh<Real>(b, p), cur, qfield<Real>(b, p, b0), b->stream);
+      launch_prim<Real>(bh<Real>(b, p), bfield<Real>(b, p, b0 ^ 1), qfield<Real>(b, p, b0 ^ 1), b->stream);
+    }
   }
   for (int k = 0; k < nsteps; ++k) {
     BatchLaunch<Real> L;
@@ -133,6 +152,7 @@ void enqueue(e2d_batch* b, int nStep0, int nsteps, int slot0, bool seed) {
     L.ctls = b->ctls;
     L.dt_log = static_cast<Real*>(b->d_dtlog) + (size_t)k * b->nprob;
     L.square = b->square;
+    L.qin = b->pool_q != nullptr;
     launch_batch_step<Real>(b->variant, L, b->stream);
   }
 }
@@ -270,6 +290,11 @@ int e2d_batch_create(const e2d_params* base, int nprob, const int* nx, const int
   cudaMemsetAsync(b->pool_u, 0, total * b->es, b->stream);
   cudaMemsetAsync(b->pool_u2, 0, total * b->es, b->stream);
   cudaMemsetAsync(b->ctls, 0, sizeof(Ctl) * (size_t)nprob, b->stream);
+  if (cudaMalloc(&b->pool_q, total * b->es) != cudaSuccess || cudaMalloc(&b->pool_q2, total * b->es) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(b->pool_q);
+    b->pool_q = b->pool_q2 = nullptr;
+  }
   if (int rc = build(b)) return cleanup(rc, "work list setup failed");
   *out = b;
   return E2D_OK;
@@ -282,6 +307,8 @@ int e2d_batch_destroy(e2d_batch* b) {
   clear_graphs(b);
   cudaFree(b->pool_u);
   cudaFree(b->pool_u2);
+  cudaFree(b->pool_q);
+  cudaFree(b->pool_q2);
   cudaFree(b->ctls);
   cudaFree(b->d_probs);
   cudaFree(b->d_dtlog);

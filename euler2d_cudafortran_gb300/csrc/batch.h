@@ -9,6 +9,8 @@ struct BatchProb {
   Hydro<Real> h;   // this problem's parameters (size, boundaries, constants)
   Real* u;         // pitched states, as a single run's u and u2
   Real* u2;
+  Real* q;         // primitives beside u and u2 (same layout), null when not kept
+  Real* q2;
   int pitch;
   long long plane;
   int ntx, nty;    // tiles of the chosen shape
@@ -25,6 +27,7 @@ struct BatchLaunch {
   const Real* dt_src = nullptr;  // if set: step with these logged dt (by problem index), no CFL fold
   Real* inv_log = nullptr;       // if set: receives each problem's running CFL maximum before the step
   bool square = false;           // every problem has dx == dy (selects the kernel that shares face sources)
+  bool qin = false;              // the boxes are read from q/q2 (current), and the step writes the next ones
 };
 
 // Tile shapes: variant 0 = 32 x 15 cells (256 threads), 1 = 32 x 7 (128 threads).

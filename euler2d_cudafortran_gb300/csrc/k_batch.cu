@@ -18,8 +18,9 @@ namespace e2d {
 namespace {
 
 // SQ: every problem of the launch has dx == dy (the shared face source term
-// of tile_compute).
-template <typename Real, class C, int MINB, bool SQ>
+// of tile_compute).  QIN: the boxes are read from the primitives kept beside
+// the states, and the update writes those of the new state (tile_compute).
+template <typename Real, class C, int MINB, bool SQ, bool QIN>
 __global__ void __launch_bounds__(C::NT, MINB)
     k_batch_step(const BatchProb<Real>* __restrict__ probs, int nprob, int total_tiles, int parity, int rd, int wr,
                  Ctl* ctls, Real* dt_log, const Real* dt_src, Real* inv_log) {
@@ -58,17 +59,20 @@ __global__ void __launch_bounds__(C::NT, MINB)
     const int i0 = GW + tx * C::TX, j0 = GW + ty * C::TY;
     Field<Real> in{parity ? P.u2 : P.u, P.pitch, P.plane};
     Field<Real> out{parity ? P.u : P.u2, P.pitch, P.plane};
-    // conservative box, zero outside the array (what TMA zero fill gives)
+    const Field<Real> box{QIN ? (parity ? P.q2 : P.q) : in.p, P.pitch, P.plane};
+    const Field<Real> qout{QIN ? (parity ? P.q : P.q2) : out.p, P.pitch, P.plane};
+    // conservative (or primitive) box, zero outside the array (what TMA zero
+    // fill gives)
     Real* sq = base + C::q_off;
     for (int k = tid; k < 4 * C::BYs * C::BXs; k += C::NT) {
       const int v = k / (C::BYs * C::BXs), rem = k - v * (C::BYs * C::BXs);
       const int y = rem / C::BXs, x = rem - y * C::BXs;
       const int gi = i0 - GW + x, gj = j0 - GW + y;
-      sq[k] = (gi < sh.isize && gj < sh.jsize) ? in.at(v, gj, gi) : Real(0);
+      sq[k] = (gi < sh.isize && gj < sh.jsize) ? box.at(v, gj, gi) : Real(0);
     }
     __syncthreads();
-    Real m = tile_compute<Real, C, SQ>(sh, base, face_counter, red, i0, j0, in, out, out, sdt[1], sdt[2], true,
-                                       wr >= 0, &ctls[id].health);
+    Real m = tile_compute<Real, C, SQ, QIN>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1], sdt[2],
+                                            true, wr >= 0, &ctls[id].health);
     if (tid == 0) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];
@@ -86,30 +90,39 @@ __global__ void __launch_bounds__(C::NT, MINB)
 
 template <typename Real, class C, int MINB>
 struct Variant {
-  template <bool SQ>
+  template <bool SQ, bool QIN>
   static int resident_sq() {
     int n = 0;
-    if (cudaFuncSetAttribute(k_batch_step<Real, C, MINB, SQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_batch_step<Real, C, MINB, SQ, QIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)C::bytes) != cudaSuccess ||
-        cudaFuncSetAttribute(k_batch_step<Real, C, MINB, SQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        cudaFuncSetAttribute(k_batch_step<Real, C, MINB, SQ, QIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<Real, C, MINB, SQ>, C::NT, C::bytes) !=
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<Real, C, MINB, SQ, QIN>, C::NT, C::bytes) !=
             cudaSuccess) {
       cudaGetLastError();
       return 0;
     }
     return n;
   }
-  // CTAs of either instantiation that fit on an SM (the persistent grid is
-  // sized by it, so it must hold for the one launched).
-  static int resident_per_sm() { return std::min(resident_sq<false>(), resident_sq<true>()); }
+  // CTAs of any instantiation that fit on an SM (the persistent grid is sized
+  // by it, so it must hold for the one launched).
+  static int resident_per_sm() {
+    return std::min(std::min(resident_sq<false, false>(), resident_sq<true, false>()),
+                    std::min(resident_sq<false, true>(), resident_sq<true, true>()));
+  }
+  template <bool SQ, bool QIN>
+  static void go(const BatchLaunch<Real>& L, cudaStream_t s) {
+    k_batch_step<Real, C, MINB, SQ, QIN><<<L.grid, C::NT, C::bytes, s>>>(
+        L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+  }
   static void launch(const BatchLaunch<Real>& L, cudaStream_t s) {
-    if (L.square)
-      k_batch_step<Real, C, MINB, true><<<L.grid, C::NT, C::bytes, s>>>(
-          L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
-    else
-      k_batch_step<Real, C, MINB, false><<<L.grid, C::NT, C::bytes, s>>>(
-          L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+    if (L.square) {
+      if (L.qin) go<true, true>(L, s);
+      else go<true, false>(L, s);
+    } else {
+      if (L.qin) go<false, true>(L, s);
+      else go<false, false>(L, s);
+    }
   }
 };
 
