@@ -55,6 +55,9 @@ struct e2d_run {
   // the next one; refreshed from u and u2 at the start of every such call.
   // Null when they could not be allocated (the step then converts its box).
   void* qprim[2] = {nullptr, nullptr};
+  // q_valid[b]: qprim[b] holds the primitives of the interior (and, unless
+  // the last writer was a per-call step, the ghosts) of buffer b.
+  bool q_valid[2] = {false, false};
   Ctl* ctl = nullptr;
   void* dt_log = nullptr;  // device
   int dt_log_cap = 0;
@@ -179,6 +182,21 @@ void enqueue_advance(e2d_run* r, int nStep0, int nsteps, int slot0, bool seed) {
     const bool bdone = (r->p.implementation_version == 0) || k == 0;
     enqueue_step<Real>(r, nStep0 + k, Real(0), true, rd, rd ^ 1, k, bdone, use_q);
   }
+}
+
+// The per-call step of implementationVersion 0 with primitive arrays: after
+// the ghost fill of the input (enqueue_step), its primitives are made current
+// -- their ghosts filled by the same rules, or both buffers' primitives formed
+// when they are not valid -- and the step writes the output's interior ones.
+template <typename Real>
+void enqueue_percall_q(e2d_run* r, int nStep, Real dt) {
+  const Hydro<Real>& h = hydro<Real>(r);
+  const int b = nStep % 2;
+  launch_boundaries<Real>(h, field<Real>(r, b ? r->u2 : r->u), r->stream);
+  if (r->q_valid[b]) launch_boundaries<Real>(h, field<Real>(r, r->qprim[b]), r->stream);
+  else refresh_prims<Real>(r, nStep);
+  enqueue_step<Real>(r, nStep, dt, false, -1, r->cur_slot, 0, true, true);
+  r->q_valid[0] = r->q_valid[1] = true;
 }
 
 template <typename Real>
@@ -369,6 +387,7 @@ int e2d_init_diagonal(e2d_run* r, double offset, double rho_hi, double p_hi, dou
   if (int rc = check_run(r)) return rc;
   if (int rc = use_device(r)) return rc;
   r->folded[0] = false;
+  r->q_valid[0] = false;
   if (r->es == 8)
     launch_init_diagonal<double>(r->hd, field<double>(r, r->u), offset, rho_hi, p_hi, rho_lo, p_lo, r->stream);
   else
@@ -390,6 +409,7 @@ int e2d_upload_state(e2d_run* r, int which, const void* host) {
   if (int rc = use_device(r)) return rc;
   const size_t w = (size_t)r->isize * r->es;
   r->folded[which] = false;
+  r->q_valid[which] = false;
   E2D_CK(cudaMemcpy2DAsync(which ? r->u2 : r->u, r->pitch * r->es, host, w, w, (size_t)4 * r->jsize,
                            cudaMemcpyHostToDevice, r->stream));
   E2D_CK(cudaStreamSynchronize(r->stream));
@@ -485,9 +505,14 @@ int e2d_make_boundaries(e2d_run* r, int which) {
   if (int rc = use_device(r)) return rc;
   if (r->es == 8) launch_boundaries<double>(r->hd, field<double>(r, which ? r->u2 : r->u), r->stream);
   else launch_boundaries<float>(r->hf, field<float>(r, which ? r->u2 : r->u), r->stream);
+  if (r->q_valid[which]) {  // the primitives' ghosts follow (a flipped momentum is a flipped velocity)
+    if (r->es == 8) launch_boundaries<double>(r->hd, field<double>(r, r->qprim[which]), r->stream);
+    else launch_boundaries<float>(r->hf, field<float>(r, r->qprim[which]), r->stream);
+  }
   E2D_CK(cudaGetLastError());
   return E2D_OK;
 }
+
 
 int e2d_godunov_unsplit(e2d_run* r, int nStep, double dt) {
   if (int rc = check_run(r)) return rc;
@@ -495,8 +520,14 @@ int e2d_godunov_unsplit(e2d_run* r, int nStep, double dt) {
   if (int rc = use_device(r)) return rc;
   // dt comes from the caller; the update epilogue folds the CFL maximum of
   // the new state into the running maximum, which the next compute_dt reads.
-  if (r->es == 8) enqueue_step<double>(r, nStep, dt, false, -1, r->cur_slot, 0, false);
-  else enqueue_step<float>(r, nStep, (float)dt, false, -1, r->cur_slot, 0, false);
+  if (r->p.implementation_version == 0 && r->qprim[0]) {
+    if (r->es == 8) enqueue_percall_q<double>(r, nStep, dt);
+    else enqueue_percall_q<float>(r, nStep, (float)dt);
+  } else if (r->es == 8) {
+    enqueue_step<double>(r, nStep, dt, false, -1, r->cur_slot, 0, false);
+  } else {
+    enqueue_step<float>(r, nStep, (float)dt, false, -1, r->cur_slot, 0, false);
+  }
   E2D_CK(cudaGetLastError());
   r->folded[(nStep % 2 == 0) ? 1 : 0] = true;
   return E2D_OK;
@@ -549,6 +580,7 @@ int e2d_advance(e2d_run* r, int nStep0, int nsteps, void* dt_log) {
   r->timed = true;
   r->cur_slot = slot0 ^ (nsteps & 1);
   r->folded[0] = r->folded[1] = true;
+  r->q_valid[0] = r->q_valid[1] = r->qprim[0] != nullptr && r->p.implementation_version == 0;
   if (dt_log) {
     E2D_CK(cudaMemcpyAsync(dt_log, r->dt_log, (size_t)nsteps * r->es, cudaMemcpyDeviceToHost, r->stream));
     E2D_CK(cudaStreamSynchronize(r->stream));
@@ -594,6 +626,7 @@ int e2d_time_steps(e2d_run* r, int nStep0, int nsteps, float* ms) {
   if (e != cudaSuccess) return cuda_fail(e, "e2d_time_steps");
   r->cur_slot = slot0 ^ (nsteps & 1);
   r->folded[0] = r->folded[1] = true;
+  r->q_valid[0] = r->q_valid[1] = use_q;
   return E2D_OK;
 }
 
@@ -634,6 +667,7 @@ int e2d_device_state(e2d_run* r, int which, void** dptr, size_t* pitch_elems, si
   if (which != 0 && which != 1) return fail(E2D_ERR_INVALID_ARG, "which must be 0 or 1");
   if (dptr) *dptr = which ? r->u2 : r->u;
   r->folded[0] = r->folded[1] = false;  // the caller may write the state directly
+  r->q_valid[0] = r->q_valid[1] = false;
   if (pitch_elems) *pitch_elems = r->pitch;
   if (plane_elems) *plane_elems = r->plane;
   return E2D_OK;

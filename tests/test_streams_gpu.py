@@ -60,3 +60,33 @@ def test_time_steps_leaves_the_advance_state(e2d, prec):
         assert b.health() == 0
     assert np.array_equal(ua, ub)
     assert inv_a == inv_b
+
+
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+def test_percall_steps_see_an_uploaded_state(e2d, prec):
+    """The per-call step keeps the primitives of its states between calls; a
+    state written from the host in between must be the one the next step
+    reads (same bits as a run that starts from it)."""
+    p = _params(e2d, 0, prec)
+    dt = 2e-4
+    with e2d.HydroRun(p) as a:
+        a.init_implode()
+        for n in range(5):
+            a.godunov_unsplit(n, dt)
+        mid = a.get_state(1)
+        mid[0, 2:-2, 2:-2] *= 1.01
+        a.set_state(1, mid)
+        a.make_boundaries(1)
+        for n in range(5, 10):
+            a.godunov_unsplit(n, dt)
+        a.make_boundaries(0)
+        ua = a.get_state(0)
+    with e2d.HydroRun(p) as b:
+        b.init_implode()
+        b.set_state(1, mid)
+        b.make_boundaries(1)
+        for n in range(5, 10):
+            b.godunov_unsplit(n, dt)
+        b.make_boundaries(0)
+        ub = b.get_state(0)
+    assert np.array_equal(ua, ub)
