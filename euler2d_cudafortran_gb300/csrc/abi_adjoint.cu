@@ -34,6 +34,10 @@ struct e2d_adjoint {
   int device = 0;
   size_t pitch = 0, plane = 0, state_elems = 0;
   double* pool = nullptr;  // states: 2 ping-pong, the checkpoints, 2 sets of K segment states
+  // the forward values of each segment state (TapeOut: 4 states' worth of
+  // elements each), written by the forward sweeps and read by the reverse
+  // steps; null when they could not be allocated (the reverse recomputes them)
+  double* tapes = nullptr;
   int nchk = 0, kseg = 0, cap_steps = 0;
   std::vector<StateMap> maps;  // one TMA descriptor per state buffer
   double* ub[3] = {nullptr, nullptr, nullptr};  // adjoint states, rotating: read, written, zeroed
@@ -66,11 +70,25 @@ Field<double> state(const e2d_adjoint* a, int k) {
 }
 Field<double> ubf(const e2d_adjoint* a, int k) { return Field<double>{a->ub[k], (int)a->pitch, (long long)a->plane}; }
 
+// The tape of segment state j of set `set`.
+TapeOut tape_of(const e2d_adjoint* a, int set, int j, bool only = false) {
+  TapeOut t;
+  t.q = a->tapes + (size_t)(set * a->kseg + j) * 4 * a->state_elems;
+  t.dq = t.q + a->state_elems;
+  t.s = t.q + 3 * a->state_elems;
+  t.pitch = (int)a->pitch;
+  t.plane = (long long)a->plane;
+  t.only = only ? 1 : 0;
+  return t;
+}
+
 void free_buffers(e2d_adjoint* a) {
   for (auto& kv : a->graphs) cudaGraphExecDestroy(kv.second);
   a->graphs.clear();
   cudaFree(a->pool);
   a->pool = nullptr;
+  cudaFree(a->tapes);
+  a->tapes = nullptr;
   cudaFree(a->dt_log);
   cudaFree(a->inv_log);
   cudaFree(a->dtbar_log);
@@ -96,6 +114,13 @@ int ensure(e2d_adjoint* a, int nsteps) {
     return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint checkpoints failed");
   }
   A_CK(cudaMemsetAsync(a->pool, 0, (size_t)nstates * a->state_elems * sizeof(double), a->stream));
+  const size_t tape_bytes = (size_t)2 * K * 4 * a->state_elems * sizeof(double);
+  if (cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    a->tapes = nullptr;
+  } else {
+    A_CK(cudaMemsetAsync(a->tapes, 0, tape_bytes, a->stream));  // cells no tile writes read as zeros
+  }
   a->maps.resize(nstates);
   for (int k = 0; k < nstates; ++k)
     if (!fused_map_create<double>(a->h, state(a, k), &a->maps[k]))
@@ -141,7 +166,11 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
     sd.wr_slot = rd ^ 1;
     sd.dt_log = a->dt_log;
     sd.log_index = k;
-    launch_fused_map<double>(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, true, s);
+    if (with_adjoint_seed && a->tapes && k >= last * K)
+      launch_fused_tape(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, tape_of(a, last & 1, k - last * K),
+                        s);
+    else
+      launch_fused_map<double>(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, true, s);
   }
   cudaMemsetAsync(a->J, 0, sizeof(double), s);
   Field<double> seed = with_adjoint_seed ? ubf(a, 0) : Field<double>{nullptr, 0, 0};
@@ -165,8 +194,25 @@ void enqueue_recompute(e2d_adjoint* a, int sg, int set, int nsteps, cudaStream_t
     sd.wr_slot = -1;
     sd.dt_log = nullptr;
     sd.log_index = 0;
-    launch_fused_map<double>(h, a->maps[seg_index(a, set, m - k0)], state(a, seg_index(a, set, m - k0)),
-                             state(a, seg_index(a, set, m - k0 + 1)), sd, a->ctl, true, s);
+    if (a->tapes)
+      launch_fused_tape(h, a->maps[seg_index(a, set, m - k0)], state(a, seg_index(a, set, m - k0)),
+                        state(a, seg_index(a, set, m - k0 + 1)), sd, a->ctl, tape_of(a, set, m - k0), s);
+    else
+      launch_fused_map<double>(h, a->maps[seg_index(a, set, m - k0)], state(a, seg_index(a, set, m - k0)),
+                               state(a, seg_index(a, set, m - k0 + 1)), sd, a->ctl, true, s);
+  }
+  if (a->tapes) {  // the segment's last state has no step here: its tape alone
+    const int j = k1 - 1 - k0;
+    StepDt<double> sd;
+    sd.dt_value = 0.0;
+    sd.dt_ptr = a->dt_log + (k1 - 1);
+    sd.from_slot = 0;
+    sd.rd_slot = -1;
+    sd.wr_slot = -1;
+    sd.dt_log = nullptr;
+    sd.log_index = 0;
+    launch_fused_tape(h, a->maps[seg_index(a, set, j)], state(a, seg_index(a, set, j)),
+                      state(a, seg_index(a, set, j)), sd, a->ctl, tape_of(a, set, j, true), s);
   }
 }
 
@@ -197,8 +243,9 @@ void enqueue_reverse(e2d_adjoint* a, int nsteps, int dt_mode) {
     for (int m = k1 - 1; m >= k0; --m) {
       const int nxt = (cur + 1) % 3, zro = (cur + 2) % 3;
       Field<double> um = state(a, seg_index(a, set, m - k0));
+      const TapeOut tp = a->tapes ? tape_of(a, set, m - k0) : TapeOut();
       launch_step_rev(h, um, ubf(a, cur), ubf(a, nxt), m > 0 ? ubf(a, zro) : Field<double>{nullptr, 0, 0},
-                      a->dt_log + m, a->dtbar_log + m, s);
+                      a->dt_log + m, a->dtbar_log + m, s, a->tapes ? &tp : nullptr);
       if (dt_mode == 1) {
         launch_argmax(h, um, a->part_v, a->part_i, a->nparts, a->inv_log, m, s);
         launch_dt_route(h, um, ubf(a, nxt), a->part_v, a->part_i, a->nparts, a->dtbar_log, a->inv_log, m, nsteps,

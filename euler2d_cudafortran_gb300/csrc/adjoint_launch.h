@@ -48,8 +48,10 @@ int step_rev_setup();
 // Ubar_n += reverse of one step (U_n with ghosts, Ubar_{n+1} interior); *dtbar += dJ/d dt.
 // dt is read on the device (the logged dt of the step).  The interior of ubz
 // (if ubz.p) is zeroed: the buffer the following reverse step accumulates into.
+// tape (if set): the forward values of U_n the forward step left (launch_fused_tape).
 void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn1, Field<double> ubn,
-                     Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s);
+                     Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s,
+                     const TapeOut* tape = nullptr);
 // Ghost corners of segment buffers seg_index + 1 .. seg_index + nseg - 1 (states k0 + j)
 // from ping-pong buffer ping_index + ((k0 + j) & 1); buffers are state_elems apart in pool.
 void launch_seg_corners(const Hydro<double>& h, double* pool, size_t state_elems, size_t pitch, size_t plane,

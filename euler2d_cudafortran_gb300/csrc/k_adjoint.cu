@@ -52,10 +52,12 @@ constexpr size_t SMEM_BYTES = (size_t)N_SMEM * sizeof(double) + 64;
 // SQ (dx == dy, so dtdx == dtdy): the face source term (s*dtd)*0.5 is formed
 // once per ring cell, and the source adjoints are summed per unit dtd and
 // scaled once per ring cell.
-template <bool SQ>
+// TAPE: the primitives of the box and the slopes and sources of the ring are
+// read from the tape the forward step wrote (TapeOut), not recomputed.
+template <bool SQ, bool TAPE = false>
 __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
                                               Field<double> ubn, Field<double> ubz, double dt, double* dtbar,
-                                              int bx, int by, double* sm) {
+                                              int bx, int by, double* sm, const TapeOut& tape = TapeOut()) {
   double* sq = sm + Q_OFF;
   double* sdq = sm + DQ_OFF;
   double* ss = sm + S_OFF;
@@ -80,7 +82,8 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   for (int k = tid; k < 4 * NBOX; k += ANT) {
     const int v = k / NBOX, rem = k - v * NBOX, y = rem / ABX, x = rem - y * ABX;
     const int gi = i0 - GW + x, gj = j0 - GW + y;
-    sq[k] = (gi < h.isize && gj < h.jsize) ? un.at(v, gj, gi) : 0.0;
+    if constexpr (TAPE) sq[k] = (gi < h.isize && gj < h.jsize) ? tape.at(tape.q, v, gj, gi) : 0.0;
+    else sq[k] = (gi < h.isize && gj < h.jsize) ? un.at(v, gj, gi) : 0.0;
     sqb[k] = 0.0;
   }
   for (int k = tid; k < 12 * NRING; k += ANT) sra[k] = 0.0;
@@ -91,6 +94,21 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     sub[k] = interior ? ubn1.at(v, gj, gi) : 0.0;
   }
   __syncthreads();
+  auto Q = [&](int v, int y, int x) -> double { return sq[(v * ABY + y) * ABX + x]; };
+  if constexpr (TAPE) {
+    for (int k = tid; k < NRING; k += ANT) {
+      const int gi = i0 - GW + k % ARX + 1, gj = j0 - GW + k / ARX + 1;
+      const bool in = gi <= h.nx + 2 && gj <= h.ny + 2;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        sdq[v * NRING + k] = in ? tape.at(tape.dq, v, gj, gi) : 0.0;
+        sdq[(4 + v) * NRING + k] = in ? tape.at(tape.dq, 4 + v, gj, gi) : 0.0;
+        const double sv = in ? tape.at(tape.s, v, gj, gi) : 0.0;
+        ss[v * NRING + k] = sv;
+        if constexpr (SQ) ssh[v * NRING + k] = Ops<double>::half(sv * dtdx);
+      }
+    }
+  } else {
   // ---- forward recomputation: primitives (box), slopes and sources (ring)
   for (int k = tid; k < NBOX; k += ANT) {
     double u[4], q[4];
@@ -101,7 +119,6 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     for (int v = 0; v < 4; ++v) sq[v * NBOX + k] = q[v];
   }
   __syncthreads();
-  auto Q = [&](int v, int y, int x) -> double { return sq[(v * ABY + y) * ABX + x]; };
   for (int k = tid; k < NRING; k += ANT) {
     const int x = k % ARX + 1, y = k / ARX + 1;
     double qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4];
@@ -119,6 +136,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       ss[v * NRING + k] = s[v];
       if constexpr (SQ) ssh[v * NRING + k] = Ops<double>::half(s[v] * dtdx);
     }
+  }
   }
   __syncthreads();
 
@@ -339,12 +357,12 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   }
 }
 
-template <bool SQ>
+template <bool SQ, bool TAPE>
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, Field<double> ubz,
-               const double* dt, double* dtbar) {
+               const double* dt, double* dtbar, TapeOut tape) {
   extern __shared__ double sm[];
-  step_rev_tile<SQ>(h, un, ubn1, ubn, ubz, *dt, dtbar, blockIdx.x, blockIdx.y, sm);
+  step_rev_tile<SQ, TAPE>(h, un, ubn1, ubn, ubz, *dt, dtbar, blockIdx.x, blockIdx.y, sm, tape);
 }
 
 // The 2x2 ghost corners are never written by a step, so a state keeps the
@@ -600,19 +618,24 @@ __global__ void k_batch_extract(const AdjProb* __restrict__ probs, int ub, doubl
 }  // namespace
 
 int step_rev_setup() {
-  return cudaFuncSetAttribute(k_step_rev<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
-                     cudaSuccess &&
-                 cudaFuncSetAttribute(k_step_rev<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)SMEM_BYTES) == cudaSuccess
-             ? 0
-             : -1;
+  bool ok = true;
+  for (auto f : {k_step_rev<false, false>, k_step_rev<true, false>, k_step_rev<false, true>, k_step_rev<true, true>})
+    ok = ok && cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) == cudaSuccess;
+  return ok ? 0 : -1;
 }
 
 void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn1, Field<double> ubn,
-                     Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s) {
+                     Field<double> ubz, const double* dt, double* dtbar, cudaStream_t s, const TapeOut* tape) {
   dim3 g((h.nx + ATX - 1) / ATX, (h.ny + ATY - 1) / ATY);
-  if (h.dx == h.dy) k_step_rev<true><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar);
-  else k_step_rev<false><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar);
+  const TapeOut t = tape ? *tape : TapeOut();
+  const bool sq = h.dx == h.dy;
+  if (tape) {
+    if (sq) k_step_rev<true, true><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
+    else k_step_rev<false, true><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
+  } else {
+    if (sq) k_step_rev<true, false><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
+    else k_step_rev<false, false><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
+  }
 }
 
 void launch_seg_corners(const Hydro<double>& h, double* pool, size_t state_elems, size_t pitch, size_t plane,

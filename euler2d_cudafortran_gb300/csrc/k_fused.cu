@@ -127,6 +127,67 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
   }
 }
 
+// The FP64 step of the adjoint's forward sweeps: k_fused (conservative box)
+// that also writes its input's primitives, slopes and trace sources to the
+// tape the reverse step reads (tile_compute, TAPE); tape.only: just the tape.
+template <bool SQ>
+__global__ void __launch_bounds__(256, E2D_FUSED_MINB64)
+    k_fused_tape(const __grid_constant__ CUtensorMap tm_in, Hydro<double> h, Field<double> in, Field<double> out,
+                 StepDt<double> sd, Ctl* ctl, TapeOut tape) {
+  using C = typename FusedTile<double>::C;
+  extern __shared__ unsigned char smem_raw[];
+  double* base = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  unsigned char* tail = reinterpret_cast<unsigned char*>(base + C::n_real);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tail);
+  int* face_counter = reinterpret_cast<int*>(tail + 8);
+  double* red = reinterpret_cast<double*>(tail + 16);
+  double* sdt = red + 32;
+  const int tid = threadIdx.x;
+  const int i0 = GW + blockIdx.x * C::TX, j0 = GW + blockIdx.y * C::TY;
+  const uint32_t bar_a = smem_u32(bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    *face_counter = 0;
+    const double dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? h.cfl / *inv_slot<double>(ctl, sd.rd_slot) : sd.dt_value;
+    sdt[0] = dt0;
+    sdt[1] = dt0 / h.dx;
+    sdt[2] = dt0 / h.dy;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(C::box_bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(smem_u32(base + C::q_off)),
+        "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
+        : "memory");
+  }
+  const double dt = sdt[0];
+  const bool ok = mbar_wait(bar_a, 0, kTmaWaitCycles);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) atomicOr(&ctl->health, 4u);
+    return;
+  }
+  const bool want_dt = sd.wr_slot >= 0 && !tape.only;
+  double m = tile_compute<double, C, SQ, false, true>(h, base, face_counter, red, i0, j0, in, out, out, sdt[1],
+                                                      sdt[2], true, want_dt, &ctl->health, nullptr, NoHook(),
+                                                      &tape);
+  if (tid == 0 && !tape.only) {
+    if (blockIdx.x == 0 && blockIdx.y == 0) {
+      if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
+      if (sd.inv_log && sd.rd_slot >= 0) sd.inv_log[sd.log_index] = *inv_slot<double>(ctl, sd.rd_slot);
+      if (!isfinite(dt)) atomicOr(&ctl->health, 1u);
+    }
+    if (want_dt) {
+      if (sd.rd_slot >= 0) m = Ops<double>::max(m, *inv_slot<double>(ctl, sd.rd_slot));
+      atomic_max_slot_ptr<double>(inv_slot<double>(ctl, sd.wr_slot), m);
+    }
+  }
+}
+
 #ifndef E2D_FUSED_PERSISTENT
 #define E2D_FUSED_PERSISTENT 1
 #endif
@@ -265,8 +326,21 @@ bool set_fused_attributes_sq() {
 
 template <typename Real>
 bool set_fused_attributes() {
-  return set_fused_attributes_sq<Real, false, false>() && set_fused_attributes_sq<Real, true, false>() &&
-         set_fused_attributes_sq<Real, false, true>() && set_fused_attributes_sq<Real, true, true>();
+  bool ok = set_fused_attributes_sq<Real, false, false>() && set_fused_attributes_sq<Real, true, false>() &&
+            set_fused_attributes_sq<Real, false, true>() && set_fused_attributes_sq<Real, true, true>();
+  if constexpr (sizeof(Real) == 8) {
+    using C = typename FusedTile<double>::C;
+    ok = ok &&
+         cudaFuncSetAttribute(k_fused_tape<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(k_fused_tape<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(k_fused_tape<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
+         cudaFuncSetAttribute(k_fused_tape<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
+  }
+  return ok;
 }
 
 template <typename Real, bool SQ, bool QIN>
@@ -389,6 +463,15 @@ void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in,
                       Ctl* ctl, bool fill_ghosts, cudaStream_t s) {
   const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(map.bytes);
   launch_fused_tm<Real>(tm, tm, h, in, out, nullptr, sd, ctl, fill_ghosts, s);
+}
+
+void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double> in, Field<double> out,
+                       StepDt<double> sd, Ctl* ctl, const TapeOut& tape, cudaStream_t s) {
+  using C = typename FusedTile<double>::C;
+  const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(map.bytes);
+  const dim3 grid((h.nx + C::TX - 1) / C::TX, (h.ny + C::TY - 1) / C::TY);
+  if (E2D_SQ_TRACE && h.dx == h.dy) k_fused_tape<true><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, tape);
+  else k_fused_tape<false><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, tape);
 }
 
 template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*);

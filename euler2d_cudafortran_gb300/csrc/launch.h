@@ -78,6 +78,28 @@ template <typename Real> void launch_fused(const Hydro<Real>& h, FusedPlan* plan
 // A TMA descriptor for any pitched state (used for states outside a run's u/u2).
 struct StateMap { alignas(64) unsigned char bytes[128]; };
 template <typename Real> bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out);
+// Where a forward step leaves the values of its input state that the reverse
+// step recomputes otherwise (the adjoint's tape): the primitives of every
+// cell, and the slopes and trace source terms of the cells the reverse's
+// rings reach (i in [1, nx+2], j in [1, ny+2]).  Pitched like a state; each
+// cell is written by exactly one tile.  only: stop after the ring pass (a
+// state whose step is not run).
+struct TapeOut {
+  double* q = nullptr;   // [4] planes
+  double* dq = nullptr;  // [8] planes: dqx[4], dqy[4]
+  double* s = nullptr;   // [4] planes
+  int pitch = 0;
+  long long plane = 0;
+  int only = 0;
+  __host__ __device__ __forceinline__ double& at(double* b, int v, int j, int i) const {
+    return b[(long long)v * plane + (long long)j * pitch + i];
+  }
+};
+
+// The adjoint's forward step: also writes its input's forward values to the
+// tape; tape.only writes just those.
+void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double> in, Field<double> out,
+                       StepDt<double> sd, Ctl* ctl, const TapeOut& tape, cudaStream_t s);
 template <typename Real> void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in,
                                                Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
                                                cudaStream_t s);

@@ -62,6 +62,14 @@ struct NoHook {
   __device__ __forceinline__ void operator()() const {}
 };
 
+// The one tile of the domain partition that owns global index g (of n interior
+// cells, first interior index GW) along one axis, for a tile starting at t0
+// of width w; ghosts (and ring ghosts) go to the edge tiles.
+__device__ __forceinline__ bool owns(int g, int t0, int w, int n) {
+  const int end = t0 + w < n + GW ? t0 + w : n + GW;
+  return (g >= t0 && g < end) || (t0 == GW && g < GW) || (t0 + w >= n + GW && g >= n + GW);
+}
+
 // box_src (optional): where the conservative box was loaded, when not in
 // place at q_off (it is then read into q_off); after_faces: run by every
 // thread right after the barrier that ends the face phase, when the slope
@@ -74,12 +82,15 @@ struct NoHook {
 // them beside its state); the update then writes the primitives of the new
 // state, and of its ghost cells, to qout.  The primitives of a state are a
 // function of its conservative values, so this changes no result.
-template <typename Real, class C, bool SQ = false, bool QIN = false, class Hook = NoHook>
+// TAPE (FP64, !QIN): the step also writes its input's forward values to
+// *tape (TapeOut).
+template <typename Real, class C, bool SQ = false, bool QIN = false, bool TAPE = false, class Hook = NoHook>
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
                                              int i0, int j0, const Field<Real>& in, const Field<Real>& out,
                                              const Field<Real>& qout, Real dtdx, Real dtdy, bool fill_ghosts,
                                              bool want_dt, unsigned* health, const Real* box_src = nullptr,
-                                             Hook after_faces = Hook()) {
+                                             Hook after_faces = Hook(), const TapeOut* tape = nullptr) {
+  static_assert(!TAPE || (sizeof(Real) == 8 && !QIN), "the tape is written by the FP64 conversion path");
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, BXs = C::BXs, BYs = C::BYs, RX = C::RX, RY = C::RY;
   Real* sq = base + C::q_off;
   Real* sdq = base + C::d_off;
@@ -99,6 +110,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       primitives(h, u, q);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sq[v * BXs * BYs + k] = q[v];
+      if constexpr (TAPE) {
+        const int gi = i0 - GW + k % BXs, gj = j0 - GW + k / BXs;
+        if (gi < h.isize && gj < h.jsize && owns(gi, i0, TX, h.nx) && owns(gj, j0, TY, h.ny)) {
+#pragma unroll
+          for (int v = 0; v < 4; ++v) tape->at(tape->q, v, gj, gi) = q[v];
+        }
+      }
     }
     __syncthreads();
   }
@@ -120,6 +138,17 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
     slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
     trace_sources(h, qc, dqx, dqy, s);
+    if constexpr (TAPE) {
+      const int gi = i0 - GW + x, gj = j0 - GW + y;
+      if (gi <= h.nx + 2 && gj <= h.ny + 2 && owns(gi, i0, TX, h.nx) && owns(gj, j0, TY, h.ny)) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          tape->at(tape->dq, v, gj, gi) = dqx[v];
+          tape->at(tape->dq, 4 + v, gj, gi) = dqy[v];
+          tape->at(tape->s, v, gj, gi) = s[v];
+        }
+      }
+    }
     if constexpr (SQ) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) s[v] = Ops<Real>::half(s[v] * dtdx);
@@ -132,6 +161,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
   }
   __syncthreads();
+  if constexpr (TAPE) {
+    if (tape->only) return Real(0);
+  }
 
   // ---- Riemann fluxes of all faces of the tile, claimed 32 at a time per
   // warp.  The y faces start on a 32-face boundary, so no warp holds faces of
