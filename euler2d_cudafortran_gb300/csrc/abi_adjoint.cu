@@ -34,9 +34,10 @@ struct e2d_adjoint {
   int device = 0;
   size_t pitch = 0, plane = 0, state_elems = 0;
   double* pool = nullptr;  // states: 2 ping-pong, the checkpoints, 2 sets of K segment states
-  // the forward values of each segment state (TapeOut: 4 states' worth of
-  // elements each), written by the forward sweeps and read by the reverse
-  // steps; null when they could not be allocated (the reverse recomputes them)
+  // the forward values of each segment state (TapeOut: primitives, slopes,
+  // sources, and the recorded HLLC solve of every face; kTapePlanes planes
+  // each), written by the forward sweeps and read by the reverse steps; null
+  // when they could not be allocated (the reverse recomputes them)
   double* tapes = nullptr;
   int nchk = 0, kseg = 0, cap_steps = 0;
   std::vector<StateMap> maps;  // one TMA descriptor per state buffer
@@ -70,12 +71,21 @@ Field<double> state(const e2d_adjoint* a, int k) {
 }
 Field<double> ubf(const e2d_adjoint* a, int k) { return Field<double>{a->ub[k], (int)a->pitch, (long long)a->plane}; }
 
+// Planes of one tape: q 4, dq 8, s 4, x and y face records HR_N each, and
+// the two planes of 32-bit face flags in one plane of doubles.
+constexpr int kTapePlanes = 4 + 8 + 4 + 2 * HR_N + 1;
+
 // The tape of segment state j of set `set`.
 TapeOut tape_of(const e2d_adjoint* a, int set, int j, bool only = false) {
   TapeOut t;
-  t.q = a->tapes + (size_t)(set * a->kseg + j) * 4 * a->state_elems;
-  t.dq = t.q + a->state_elems;
-  t.s = t.q + 3 * a->state_elems;
+  double* b = a->tapes + (size_t)(set * a->kseg + j) * kTapePlanes * a->plane;
+  t.q = b;
+  t.dq = b + 4 * a->plane;
+  t.s = b + 12 * a->plane;
+  t.fx = b + 16 * a->plane;
+  t.fy = t.fx + HR_N * a->plane;
+  t.flx = reinterpret_cast<unsigned*>(t.fy + HR_N * a->plane);
+  t.fly = t.flx + a->plane;
   t.pitch = (int)a->pitch;
   t.plane = (long long)a->plane;
   t.only = only ? 1 : 0;
@@ -114,7 +124,7 @@ int ensure(e2d_adjoint* a, int nsteps) {
     return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint checkpoints failed");
   }
   A_CK(cudaMemsetAsync(a->pool, 0, (size_t)nstates * a->state_elems * sizeof(double), a->stream));
-  const size_t tape_bytes = (size_t)2 * K * 4 * a->state_elems * sizeof(double);
+  const size_t tape_bytes = (size_t)2 * K * kTapePlanes * a->plane * sizeof(double);
   if (cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
     cudaGetLastError();
     a->tapes = nullptr;

@@ -17,9 +17,7 @@ namespace adj {
 
 using O = Ops<double>;
 
-#ifndef E2D_REV_ONESTAR
-#define E2D_REV_ONESTAR 1
-#endif
+
 
 __device__ __forceinline__ bool picks_first_max(double a, double b) { return emul::gt_i(a, b); }  // max(a,b) == a
 __device__ __forceinline__ bool picks_first_min(double a, double b) { return emul::ord(a) < emul::ord(b); }
@@ -150,71 +148,28 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
   }
 }
 
-// riemann_2d_hllc (serial_ref/m_utils.f90:534-644) reverse: fb -> (qlb, qrb).
-// Also returns the forward flux (bit for bit riemann_hllc's) in flux[4].
-__device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const double ql[4], const double qr[4],
-                                                 const double fb[4], double qlb[4], double qrb[4],
-                                                 double flux[4]) {
-  // ---- forward recomputation (same operations and branches as riemann_hllc)
-  const double rl = O::max(ql[ID], h.smallr), rr = O::max(qr[ID], h.smallr);
-  bool pl_raw, pr_raw;  // the pressure floors returned the face pressures
-  const double pl = floor_pick(ql[IP], rl, h.smallp, pl_raw), pr = floor_pick(qr[IP], rr, h.smallp, pr_raw);
-  const double ul = ql[IU], ur = qr[IU], vl = ql[IV], vr = qr[IV];
-  const double hrl = O::half(rl), hrr = O::half(rr);
-  const double etotl = (pl * h.entho) + (((hrl * ul) * ul) + ((hrl * vl) * vl));
-  const double etotr = (pr * h.entho) + (((hrr * ur) * ur) + ((hrr * vr) * vr));
-  const double cal = O::div(h.gamma0 * pl, rl), car = O::div(h.gamma0 * pr, rr);
-  const bool cl_act = picks_first_max(cal, h.smallc2), cr_act = picks_first_max(car, h.smallc2);
-  const double cfastl = O::sqrt(cl_act ? cal : h.smallc2), cfastr = O::sqrt(cr_act ? car : h.smallc2);
-  const bool cmax_l = picks_first_max(cfastl, cfastr);
-  const double cmax = cmax_l ? cfastl : cfastr;
-  const bool min_l = picks_first_min(ul, ur), max_l = picks_first_max(ul, ur);
-  const double SL = (min_l ? ul : ur) - cmax;
-  const double SR = (max_l ? ul : ur) + cmax;
-  const double rcl = rl * (ul - SL), rcr = rr * (SR - ur);
-  const double den = rcr + rcl;
-  const double ustar = O::div(((rcr * ur) + (rcl * ul)) + (pl - pr), den);
-  const double ptotstar = O::div(((rcr * pl) + (rcl * pr)) + ((rcl * rcr) * (ul - ur)), den);
-#if E2D_REV_ONESTAR
-  // The sampled side K first (SL > 0: left state; ustar > 0: left star;
-  // SR > 0: right star; else right state), then one star state from its
-  // values: a warp whose faces sample both stars issues the arithmetic once.
-  const bool b1 = O::gt0(SL), b2 = !b1 && O::gt0(ustar);
-  const bool star = b2 || (!b1 && O::gt0(SR));
-  const bool lside = b1 || b2;
+// riemann_2d_hllc (serial_ref/m_utils.f90:534-644) reverse from the solve's
+// recorded forward values (riemann_hllc_rec): fb -> (qlb, qrb), "+=".
+__device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, const double* rec, unsigned flags,
+                                                     const double fb[4], double qlb[4], double qrb[4]) {
+  const double ul = rec[HR_QL + IU], ur = rec[HR_QR + IU], vl = rec[HR_QL + IV], vr = rec[HR_QR + IV];
+  const double rl = O::max(rec[HR_QL + ID], h.smallr), rr = O::max(rec[HR_QR + ID], h.smallr);
+  const double pl = rec[HR_PL], pr = rec[HR_PR];
+  const double etotl = rec[HR_ETOTL], etotr = rec[HR_ETOTR], cal = rec[HR_CAL], car = rec[HR_CAR];
+  const double cfastl = rec[HR_CFL], cfastr = rec[HR_CFR], SL = rec[HR_SL], SR = rec[HR_SR];
+  const double rcl = rec[HR_RCL], rcr = rec[HR_RCR], ustar = rec[HR_USTAR], ptotstar = rec[HR_PSTAR];
+  const double ro = rec[HR_RO], etoto = rec[HR_ETOTO], fr = rec[HR_FLUX + ID];
+  const bool pl_raw = flags & HF_PL_RAW, pr_raw = flags & HF_PR_RAW;
+  const bool cl_act = flags & HF_CL_ACT, cr_act = flags & HF_CR_ACT, cmax_l = flags & HF_CMAX_L;
+  const bool min_l = flags & HF_MIN_L, max_l = flags & HF_MAX_L, vleft = flags & HF_VLEFT;
+  const bool b1 = flags & HF_B1, b2 = flags & HF_B2, b3 = flags & HF_B3;
+  const bool star = b2 || b3, lside = b1 || b2;  // sampled side K: left for branches 1, 2
   const double SK = lside ? SL : SR, rK = lside ? rl : rr, uK = lside ? ul : ur;
   const double eK = lside ? etotl : etotr, pK = lside ? pl : pr;
-  double ro = rK, uo = uK, ptoto = pK, etoto = eK, d = 1.0, dS = 0.0;
-  if (star) {
-    dS = SK - uK;
-    d = SK - ustar;
-    ro = O::div(rK * dS, d); uo = ustar; ptoto = ptotstar;
-    etoto = O::div((((dS * eK) - (pK * uK)) + (ptotstar * ustar)), d);
-  }
-#else
-  int branch;
-  double ro, uo, ptoto, etoto, d = 1.0, nE = 0.0;
-  if (O::gt0(SL)) { branch = 1; ro = rl; uo = ul; ptoto = pl; etoto = etotl; }
-  else if (O::gt0(ustar)) {
-    branch = 2; d = SL - ustar;
-    ro = O::div(rl * (SL - ul), d); uo = ustar; ptoto = ptotstar;
-    nE = (((SL - ul) * etotl) - (pl * ul)) + (ptotstar * ustar); etoto = O::div(nE, d);
-  } else if (O::gt0(SR)) {
-    branch = 3; d = SR - ustar;
-    ro = O::div(rr * (SR - ur), d); uo = ustar; ptoto = ptotstar;
-    nE = (((SR - ur) * etotr) - (pr * ur)) + (ptotstar * ustar); etoto = O::div(nE, d);
-  } else { branch = 4; ro = rr; uo = ur; ptoto = pr; etoto = etotr; }
-#endif
-  const double fr = ro * uo;
-  const bool vleft = O::gt0(fr);
-  flux[ID] = fr;
-  flux[IU] = (fr * uo) + ptoto;
-  flux[IP] = (etoto + ptoto) * uo;
-  flux[IV] = fr * (vleft ? vl : vr);
+  const double uo = star ? ustar : uK, ptoto = star ? ptotstar : pK;
+  const double den = rcr + rcl;
 
-  // ---- reverse
-  double rlb = 0, rrb = 0, plb = 0, prb = 0, ulb = 0, urb = 0, vlb = 0, vrb = 0, etotlb = 0, etotrb = 0;
-  double SLb = 0, SRb = 0, ustarb = 0, ptotstarb = 0;
+  double rlb, rrb, plb, prb, ulb, urb, vlb = 0, vrb = 0, etotlb, etotrb, SLb, SRb, ustarb = 0, ptotstarb = 0;
   // flux[IV] = fr * (vl or vr)
   double frb = fb[ID] + fb[IV] * (vleft ? vl : vr);
   if (vleft) vlb += fb[IV] * fr; else vrb += fb[IV] * fr;
@@ -226,10 +181,11 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   // fr = ro * uo
   double rob = frb * uo;
   uob += frb * ro;
-#if E2D_REV_ONESTAR
   {
+    // one star state for either side: a warp whose faces sample both issues it once
     double rKb = rob, uKb = uob, pKb = ptotob, eKb = etotob, SKb = 0.0;
     if (star) {
+      const double dS = SK - uK, d = SK - ustar;
       ustarb += uob; ptotstarb += ptotob;
       const double rq = O::div(rob, d);
       rKb = rq * dS; SKb = rq * rK; uKb = O::neg_if(rq * rK, true);
@@ -239,41 +195,12 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
       pKb = O::neg_if(nEb * uK, true); uKb -= nEb * pK; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
       SKb += db; ustarb -= db;
     }
-    // the side's accumulators are all zero here: route by selection
     rlb = lside ? rKb : 0.0; rrb = lside ? 0.0 : rKb;
     ulb = lside ? uKb : 0.0; urb = lside ? 0.0 : uKb;
     plb = lside ? pKb : 0.0; prb = lside ? 0.0 : pKb;
     etotlb = lside ? eKb : 0.0; etotrb = lside ? 0.0 : eKb;
     SLb = lside ? SKb : 0.0; SRb = lside ? 0.0 : SKb;
   }
-#else
-  switch (branch) {
-    case 1: rlb += rob; ulb += uob; plb += ptotob; etotlb += etotob; break;
-    case 4: rrb += rob; urb += uob; prb += ptotob; etotrb += etotob; break;
-    case 2: {
-      ustarb += uob; ptotstarb += ptotob;
-      const double rq = O::div(rob, d);
-      rlb += rq * (SL - ul); SLb += rq * rl; ulb -= rq * rl;
-      const double nEb = O::div(etotob, d);
-      const double db = O::neg_if(rq * ro + nEb * etoto, true);  // d(ro, etoto)/d(d)
-      SLb += nEb * etotl; ulb -= nEb * etotl; etotlb += nEb * (SL - ul);
-      plb -= nEb * ul; ulb -= nEb * pl; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
-      SLb += db; ustarb -= db;
-      break;
-    }
-    default: {  // 3
-      ustarb += uob; ptotstarb += ptotob;
-      const double rq = O::div(rob, d);
-      rrb += rq * (SR - ur); SRb += rq * rr; urb -= rq * rr;
-      const double nEb = O::div(etotob, d);
-      const double db = O::neg_if(rq * ro + nEb * etoto, true);
-      SRb += nEb * etotr; urb -= nEb * etotr; etotrb += nEb * (SR - ur);
-      prb -= nEb * ur; urb -= nEb * pr; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
-      SRb += db; ustarb -= db;
-      break;
-    }
-  }
-#endif
   // ptotstar and ustar = num / den
   const double npb = O::div(ptotstarb, den), nub = O::div(ustarb, den);
   double denb = -npb * ptotstar - nub * ustar;
@@ -312,10 +239,23 @@ __device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const d
   // pressure and density floors
   if (pl_raw) qlb[IP] += plb; else rlb += plb * h.smallp;
   if (pr_raw) qrb[IP] += prb; else rrb += prb * h.smallp;
-  if (picks_first_max(ql[ID], h.smallr)) qlb[ID] += rlb;
-  if (picks_first_max(qr[ID], h.smallr)) qrb[ID] += rrb;
+  if (emul::gt_i(rec[HR_QL + ID], h.smallr)) qlb[ID] += rlb;
+  if (emul::gt_i(rec[HR_QR + ID], h.smallr)) qrb[ID] += rrb;
   qlb[IU] += ulb; qlb[IV] += vlb;
   qrb[IU] += urb; qrb[IV] += vrb;
+}
+
+// The same, recomputing the forward values from the face states; returns
+// the forward flux (bit for bit riemann_hllc's) in flux[4].
+__device__ __forceinline__ void riemann_hllc_rev(const Hydro<double>& h, const double ql[4], const double qr[4],
+                                                 const double fb[4], double qlb[4], double qrb[4],
+                                                 double flux[4]) {
+  double rec[HR_N];
+  unsigned flags;
+  riemann_hllc_rec(h, ql, qr, rec, flags);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) flux[v] = rec[HR_FLUX + v];
+  riemann_hllc_rev_rec(h, rec, flags, fb, qlb, qrb);
 }
 
 }  // namespace adj

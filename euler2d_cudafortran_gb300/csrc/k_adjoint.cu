@@ -52,8 +52,9 @@ constexpr size_t SMEM_BYTES = (size_t)N_SMEM * sizeof(double) + 64;
 // SQ (dx == dy, so dtdx == dtdy): the face source term (s*dtd)*0.5 is formed
 // once per ring cell, and the source adjoints are summed per unit dtd and
 // scaled once per ring cell.
-// TAPE: the primitives of the box and the slopes and sources of the ring are
-// read from the tape the forward step wrote (TapeOut), not recomputed.
+// TAPE: the primitives of the box, the slopes and sources of the ring and
+// each face's HLLC solve are read from the tape the forward step wrote
+// (TapeOut, face records required), not recomputed.
 template <bool SQ, bool TAPE = false>
 __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
                                               Field<double> ubn, Field<double> ubz, double dt, double* dtbar,
@@ -161,11 +162,13 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     const int nf = xface ? nfx * ATY : (par ? NGY_ODD : NGY_EVEN) * ATX;
     int a = 0, b = 0;  // ring indices of the two cells (left/lower, right/upper)
     int ia = 0, ja = 0;
+    int fi = 0, fj = 0;  // the face's cell to its right / above it
     double fb[4];
     bool valid = tid < nf;
     if (xface) {
       const int f = 2 * (tid % nfx) + par, r = tid / nfx;
       const int i = i0 + f, j = j0 + r;
+      fi = i; fj = j;
       valid = valid && i <= h.nx + 2 && j <= h.ny + 1 && (f < ATX || i == h.nx + 2);
 #pragma unroll
       for (int v = 0; v < 4; ++v) fb[v] = valid ? UB(v, i, j) - UB(v, i - 1, j) : 0.0;
@@ -175,6 +178,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     } else {
       const int c = tid % ATX, g = 2 * (tid / ATX) + par;
       const int i = i0 + c, j = j0 + g;
+      fi = i; fj = j;
       valid = valid && i <= h.nx + 1 && j <= h.ny + 2 && (g < ATY || j == h.ny + 2);
 #pragma unroll
       for (int v = 0; v < 4; ++v) fb[v] = valid ? UB(v, i, j) - UB(v, i, j - 1) : 0.0;
@@ -185,7 +189,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
     if (valid) {
       const double dtd = xface ? dtdx : dtdy;
       const int nrm = xface ? 0 : 4;  // slope block of the face normal
-      double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], sha[4], shb[4], ql[4], qr[4];
+      double qa[4], qb_[4], dqa[4], dqb[4], sa[4], sb[4], sha[4], shb[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         qa[v] = Q(v, ja, ia);
@@ -193,17 +197,6 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
         dqa[v] = sdq[(nrm + v) * NRING + a]; dqb[v] = sdq[(nrm + v) * NRING + b];
         sa[v] = ss[v * NRING + a]; sb[v] = ss[v * NRING + b];
         if constexpr (SQ) { sha[v] = ssh[v * NRING + a]; shb[v] = ssh[v * NRING + b]; }
-      }
-      if constexpr (SQ) {
-        trace_face<double, true, true>(h, qa, dqa, sha, dtd, ql);
-        trace_face<double, false, true>(h, qb_, dqb, shb, dtd, qr);
-      } else {
-        trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
-        trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
-      }
-      if (!xface) {
-        double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
-        t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
       }
       double rb[4];
       if (xface) {
@@ -213,7 +206,30 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
         rb[ID] = fb[ID] * dtd; rb[IP] = fb[IP] * dtd; rb[IU] = fb[IV] * dtd; rb[IV] = fb[IU] * dtd;
       }
       double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0}, flux[4];
-      adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb, flux);
+      if constexpr (TAPE) {  // the face's solve, recorded by the forward step
+        double rec[HR_N];
+        double* fr = xface ? tape.fx : tape.fy;
+#pragma unroll
+        for (int e = 0; e < HR_N; ++e) rec[e] = tape.at(fr, e, fj, fi);
+        const unsigned fl = tape.flag(xface ? tape.flx : tape.fly, fj, fi);
+        adj::riemann_hllc_rev_rec(h, rec, fl, rb, qlb, qrb);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) flux[v] = rec[HR_FLUX + v];
+      } else {
+        double ql[4], qr[4];
+        if constexpr (SQ) {
+          trace_face<double, true, true>(h, qa, dqa, sha, dtd, ql);
+          trace_face<double, false, true>(h, qb_, dqb, shb, dtd, qr);
+        } else {
+          trace_face<double, true>(h, qa, dqa, sa, dtd, ql);
+          trace_face<double, false>(h, qb_, dqb, sb, dtd, qr);
+        }
+        if (!xface) {
+          double t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
+          t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
+        }
+        adj::riemann_hllc_rev(h, ql, qr, rb, qlb, qrb, flux);
+      }
       if (xface) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) dtdxb += flux[v] * fb[v];

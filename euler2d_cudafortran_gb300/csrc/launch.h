@@ -81,16 +81,27 @@ template <typename Real> bool fused_map_create(const Hydro<Real>& h, Field<Real>
 // Where a forward step leaves the values of its input state that the reverse
 // step recomputes otherwise (the adjoint's tape): the primitives of every
 // cell, and the slopes and trace source terms of the cells the reverse's
-// rings reach (i in [1, nx+2], j in [1, ny+2]).  Pitched like a state; each
-// cell is written by exactly one tile.  only: stop after the ring pass (a
+// rings reach (i in [1, nx+2], j in [1, ny+2]), and optionally each face's
+// HLLC solve.  Pitched like a state; each cell and face is written by exactly
+// one tile.  only: stop before the update (a
 // state whose step is not run).
 struct TapeOut {
   double* q = nullptr;   // [4] planes
   double* dq = nullptr;  // [8] planes: dqx[4], dqy[4]
   double* s = nullptr;   // [4] planes
+  // optional: the recorded HLLC solve of every face (physics.cuh, HR_*
+  // planes and a plane of HF_* flags), x faces at the cell to their right,
+  // y faces at the cell above them
+  double* fx = nullptr;
+  double* fy = nullptr;
+  unsigned* flx = nullptr;
+  unsigned* fly = nullptr;
   int pitch = 0;
   long long plane = 0;
   int only = 0;
+  __host__ __device__ __forceinline__ unsigned& flag(unsigned* b, int j, int i) const {
+    return b[(long long)j * pitch + i];
+  }
   __host__ __device__ __forceinline__ double& at(double* b, int v, int j, int i) const {
     return b[(long long)v * plane + (long long)j * pitch + i];
   }

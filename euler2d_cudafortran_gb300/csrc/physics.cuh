@@ -468,6 +468,87 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   flux[IV] = flux[ID] * (O::gt0(flux[ID]) ? qleft[IV] : qright[IV]);  // one product, either way
 }
 
+// The forward values of one HLLC solve that its reverse needs (the adjoint's
+// face tape), in the order riemann_hllc_rec stores them.
+enum {
+  HR_QL = 0, HR_QR = 4, HR_PL = 8, HR_PR, HR_ETOTL, HR_ETOTR, HR_CAL, HR_CAR, HR_CFL, HR_CFR, HR_SL, HR_SR,
+  HR_RCL, HR_RCR, HR_USTAR, HR_PSTAR, HR_RO, HR_ETOTO, HR_FLUX, HR_N = HR_FLUX + 4
+};
+// flag bits: which operand each max/min, floor and branch of the solve took
+enum {
+  HF_PL_RAW = 1, HF_PR_RAW = 2, HF_CL_ACT = 4, HF_CR_ACT = 8, HF_CMAX_L = 16, HF_MIN_L = 32, HF_MAX_L = 64,
+  HF_B1 = 128, HF_B2 = 256, HF_B3 = 512, HF_VLEFT = 1024
+};
+
+// riemann_hllc for double, recording its forward values into rec[HR_N] and
+// flags (bit for bit the same flux: the same operations in the same order,
+// with each max/min written as the selection it makes).
+__device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const double qleft[4],
+                                                 const double qright[4], double rec[HR_N], unsigned& flags) {
+  using O = Ops<double>;
+  const auto pmax = [](double a, double b) { return emul::gt_i(a, b); };            // max(a, b) returns a
+  const auto pmin = [](double a, double b) { return emul::ord(a) < emul::ord(b); };  // min(a, b) returns a
+  bool pl_raw, pr_raw;
+  const double rl = O::max(qleft[ID], h.smallr);
+  const double pl = floor_pick(qleft[IP], rl, h.smallp, pl_raw);
+  const double ul = qleft[IU];
+  const double hrl = O::half(rl);
+  double ecinl = (hrl * ul) * ul;
+  ecinl = ecinl + ((hrl * qleft[IV]) * qleft[IV]);
+  const double etotl = (pl * h.entho) + ecinl;
+  const double rr = O::max(qright[ID], h.smallr);
+  const double pr = floor_pick(qright[IP], rr, h.smallp, pr_raw);
+  const double ur = qright[IU];
+  const double hrr = O::half(rr);
+  double ecinr = (hrr * ur) * ur;
+  ecinr = ecinr + ((hrr * qright[IV]) * qright[IV]);
+  const double etotr = (pr * h.entho) + ecinr;
+  const double cal = O::div(h.gamma0 * pl, rl), car = O::div(h.gamma0 * pr, rr);
+  const bool cl_act = pmax(cal, h.smallc2), cr_act = pmax(car, h.smallc2);
+  const double cfastl = O::sqrt(cl_act ? cal : h.smallc2);
+  const double cfastr = O::sqrt(cr_act ? car : h.smallc2);
+  const bool cmax_l = pmax(cfastl, cfastr);
+  const double cmax = cmax_l ? cfastl : cfastr;
+  const bool min_l = pmin(ul, ur), max_l = pmax(ul, ur);
+  const double SL = (min_l ? ul : ur) - cmax;
+  const double SR = (max_l ? ul : ur) + cmax;
+  const double rcl = rl * (ul - SL);
+  const double rcr = rr * (SR - ur);
+  const double ustar = O::div(((rcr * ur) + (rcl * ul)) + (pl - pr), rcr + rcl);
+  const double ptotstar = O::div(((rcr * pl) + (rcl * pr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
+  double ro, uo, ptoto, etoto;
+  const bool b1 = O::gt0(SL), b2 = !b1 && O::gt0(ustar), b3 = !b1 && !b2 && O::gt0(SR);
+  if (b1) {
+    ro = rl; uo = ul; ptoto = pl; etoto = etotl;
+  } else if (b2) {
+    ro = O::div(rl * (SL - ul), SL - ustar);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div((((SL - ul) * etotl) - (pl * ul)) + (ptotstar * ustar), SL - ustar);
+  } else if (b3) {
+    ro = O::div(rr * (SR - ur), SR - ustar);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div((((SR - ur) * etotr) - (pr * ur)) + (ptotstar * ustar), SR - ustar);
+  } else {
+    ro = rr; uo = ur; ptoto = pr; etoto = etotr;
+  }
+  const double f0 = ro * uo;
+  const bool vleft = O::gt0(f0);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) { rec[HR_QL + v] = qleft[v]; rec[HR_QR + v] = qright[v]; }
+  rec[HR_PL] = pl; rec[HR_PR] = pr; rec[HR_ETOTL] = etotl; rec[HR_ETOTR] = etotr;
+  rec[HR_CAL] = cal; rec[HR_CAR] = car; rec[HR_CFL] = cfastl; rec[HR_CFR] = cfastr;
+  rec[HR_SL] = SL; rec[HR_SR] = SR; rec[HR_RCL] = rcl; rec[HR_RCR] = rcr;
+  rec[HR_USTAR] = ustar; rec[HR_PSTAR] = ptotstar; rec[HR_RO] = ro; rec[HR_ETOTO] = etoto;
+  rec[HR_FLUX + ID] = f0;
+  rec[HR_FLUX + IU] = ((ro * uo) * uo) + ptoto;
+  rec[HR_FLUX + IP] = (etoto + ptoto) * uo;
+  rec[HR_FLUX + IV] = f0 * (vleft ? qleft[IV] : qright[IV]);
+  flags = (pl_raw ? HF_PL_RAW : 0u) | (pr_raw ? HF_PR_RAW : 0u) | (cl_act ? HF_CL_ACT : 0u) |
+          (cr_act ? HF_CR_ACT : 0u) | (cmax_l ? HF_CMAX_L : 0u) | (min_l ? HF_MIN_L : 0u) |
+          (max_l ? HF_MAX_L : 0u) | (b1 ? HF_B1 : 0u) | (b2 ? HF_B2 : 0u) | (b3 ? HF_B3 : 0u) |
+          (vleft ? HF_VLEFT : 0u);
+}
+
 template <typename Real>
 __device__ __forceinline__ void riemann(const Hydro<Real>& h, const Real ql[4], const Real qr[4], Real flux[4]) {
   if (h.riemann == 2) riemann_hllc(h, ql, qr, flux);

@@ -161,9 +161,6 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
   }
   __syncthreads();
-  if constexpr (TAPE) {
-    if (tape->only) return Real(0);
-  }
 
   // ---- Riemann fluxes of all faces of the tile, claimed 32 at a time per
   // warp.  The y faces start on a 32-face boundary, so no warp holds faces of
@@ -193,7 +190,24 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
 #pragma unroll
         for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 2); dq[v] = sdq[v * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
         trace_face<Real, false, SQ>(h, qc, dq, s, dtdx, qr);
-        riemann(h, ql, qr, flux);
+        if constexpr (TAPE) {
+          if (tape->fx) {
+            double rec[HR_N];
+            unsigned fl;
+            riemann_hllc_rec(h, ql, qr, rec, fl);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) flux[v] = rec[HR_FLUX + v];
+            if (f < TX || i0 + TX == h.nx + 2) {  // the face at the left of cell (i0 + f, j0 + r)
+#pragma unroll
+              for (int e = 0; e < HR_N; ++e) tape->at(tape->fx, e, j0 + r, i0 + f) = rec[e];
+              tape->flag(tape->flx, j0 + r, i0 + f) = fl;
+            }
+          } else {
+            riemann(h, ql, qr, flux);
+          }
+        } else {
+          riemann(h, ql, qr, flux);
+        }
 #pragma unroll
         for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = flux[v] * dtdx;
       }
@@ -211,7 +225,24 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         trace_face<Real, false, SQ>(h, qc, dq, s, dtdy, qr);
         Real t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
         t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
-        riemann(h, ql, qr, flux);
+        if constexpr (TAPE) {
+          if (tape->fy) {
+            double rec[HR_N];
+            unsigned fl;
+            riemann_hllc_rec(h, ql, qr, rec, fl);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) flux[v] = rec[HR_FLUX + v];
+            if (g < TY || j0 + TY == h.ny + 2) {  // the face below cell (i0 + c, j0 + g)
+#pragma unroll
+              for (int e = 0; e < HR_N; ++e) tape->at(tape->fy, e, j0 + g, i0 + c) = rec[e];
+              tape->flag(tape->fly, j0 + g, i0 + c) = fl;
+            }
+          } else {
+            riemann(h, ql, qr, flux);
+          }
+        } else {
+          riemann(h, ql, qr, flux);
+        }
         t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
 #pragma unroll
         for (int v = 0; v < 4; ++v) sfy[(v * (TY + 1) + g) * TX + c] = flux[v] * dtdy;
@@ -219,6 +250,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
   }
   __syncthreads();
+  if constexpr (TAPE) {
+    if (tape->only) return Real(0);
+  }
   after_faces();
 
   // ---- updateHydro + ghost copies + next-step CFL maximum
