@@ -39,6 +39,12 @@ struct e2d_adjoint {
   // each), written by the forward sweeps and read by the reverse steps; null
   // when they could not be allocated (the reverse recomputes them)
   double* tapes = nullptr;
+  // primitives beside the two forward ping-pong states (the fast forward step
+  // of e2d_advance: the step reads its input's and writes its output's);
+  // null when they could not be allocated
+  double* qping = nullptr;
+  StateMap qmaps[2];
+  std::map<std::tuple<int, double, double, double>, cudaGraphExec_t> fwd_graphs;
   int nchk = 0, kseg = 0, cap_steps = 0;
   std::vector<StateMap> maps;  // one TMA descriptor per state buffer
   double* ub[3] = {nullptr, nullptr, nullptr};  // adjoint states, rotating: read, written, zeroed
@@ -92,9 +98,15 @@ TapeOut tape_of(const e2d_adjoint* a, int set, int j, bool only = false) {
   return t;
 }
 
+Field<double> qpf(const e2d_adjoint* a, int k) {
+  return Field<double>{a->qping + (size_t)k * a->state_elems, (int)a->pitch, (long long)a->plane};
+}
+
 void free_buffers(e2d_adjoint* a) {
   for (auto& kv : a->graphs) cudaGraphExecDestroy(kv.second);
   a->graphs.clear();
+  for (auto& kv : a->fwd_graphs) cudaGraphExecDestroy(kv.second);
+  a->fwd_graphs.clear();
   cudaFree(a->pool);
   a->pool = nullptr;
   cudaFree(a->tapes);
@@ -155,6 +167,10 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
   cudaMemsetAsync(a->ctl, 0, sizeof(Ctl), s);
   launch_dt_reduce<double>(h, state(a, kPing), a->ctl, 0, s);  // main.f90:42
   launch_boundaries<double>(h, state(a, kPing), s);            // main.f90:46
+  if (a->qping) {  // the primitives of both ping-pong states (the second for its corners)
+    launch_prim<double>(h, state(a, kPing), qpf(a, 0), s);
+    launch_prim<double>(h, state(a, kPing + 1), qpf(a, 1), s);
+  }
   const int K = a->kseg, last = (nsteps + K - 1) / K - 1;
   for (int k = 0; k < nsteps; ++k) {
     const int in = k & 1, out = in ^ 1;
@@ -176,9 +192,12 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
     sd.wr_slot = rd ^ 1;
     sd.dt_log = a->dt_log;
     sd.log_index = k;
+    // (the tape steps are the last segment's: no primitives-reading step follows them)
     if (with_adjoint_seed && a->tapes && k >= last * K)
       launch_fused_tape(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, tape_of(a, last & 1, k - last * K),
                         s);
+    else if (a->qping)
+      launch_fused_map_q(h, a->qmaps[in], state(a, in), state(a, out), qpf(a, out), sd, a->ctl, s);
     else
       launch_fused_map<double>(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, true, s);
   }
@@ -324,6 +343,15 @@ int e2d_adjoint_create(const e2d_params* p, e2d_adjoint** out) {
     e2d_adjoint_destroy(a);
     return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint state failed");
   }
+  if (cudaMalloc(&a->qping, 2 * sb) != cudaSuccess) {
+    cudaGetLastError();
+    a->qping = nullptr;
+  } else if (!fused_map_create<double>(a->h, qpf(a, 0), &a->qmaps[0]) ||
+             !fused_map_create<double>(a->h, qpf(a, 1), &a->qmaps[1])) {
+    cudaGetLastError();
+    cudaFree(a->qping);
+    a->qping = nullptr;
+  }
   if (cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&a->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&a->e0) != cudaSuccess || cudaEventCreate(&a->e1) != cudaSuccess ||
@@ -344,6 +372,7 @@ int e2d_adjoint_destroy(e2d_adjoint* a) {
   cudaFree(a->ub[0]);
   cudaFree(a->ub[1]);
   cudaFree(a->ub[2]);
+  cudaFree(a->qping);
   cudaFree(a->ctl);
   cudaFree(a->J);
   cudaFree(a->part_v);
@@ -367,8 +396,33 @@ int e2d_adjoint_objective(e2d_adjoint* a, const void* u0, int nsteps, double xc,
   cudaSetDevice(a->device);
   if (int rc = ensure(a, nsteps)) return rc;
   if (int rc = load_initial(a, u0)) return rc;
+  // replayed from a captured graph on later calls with the same step count and
+  // objective (not with given dt values)
+  cudaGraphExec_t exec = nullptr;
+  if (!dt_fixed) {
+    const auto key = std::make_tuple(nsteps, xc, yc, sigma);
+    auto it = a->fwd_graphs.find(key);
+    if (it != a->fwd_graphs.end()) {
+      exec = it->second;
+    } else {
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(a->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        enqueue_forward(a, nsteps, xc, yc, sigma, false, nullptr);
+        if (cudaStreamEndCapture(a->stream, &graph) == cudaSuccess && graph) {
+          if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+          cudaGraphDestroy(graph);
+        }
+      }
+      cudaGetLastError();
+      if (exec) {
+        cudaGraphUpload(exec, a->stream);
+        a->fwd_graphs[key] = exec;
+      }
+    }
+  }
   A_CK(cudaEventRecord(a->e0, a->stream));
-  enqueue_forward(a, nsteps, xc, yc, sigma, false, dt_fixed);
+  if (exec) A_CK(cudaGraphLaunch(exec, a->stream));
+  else enqueue_forward(a, nsteps, xc, yc, sigma, false, dt_fixed);
   A_CK(cudaGetLastError());
   A_CK(cudaEventRecord(a->e1, a->stream));
   A_CK(cudaMemcpyAsync(J, a->J, sizeof(double), cudaMemcpyDeviceToHost, a->stream));

@@ -474,6 +474,12 @@ void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double
   else k_fused_tape<false><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, tape);
 }
 
+void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, Field<double> in, Field<double> out,
+                        Field<double> qout, StepDt<double> sd, Ctl* ctl, cudaStream_t s) {
+  const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(qmap.bytes);
+  launch_fused_tm<double>(tm, tm, h, in, out, &qout, sd, ctl, true, s);
+}
+
 template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*);
 template bool fused_map_create<float>(const Hydro<float>&, Field<float>, StateMap*);
 template void launch_fused_map<double>(const Hydro<double>&, const StateMap&, Field<double>, Field<double>,

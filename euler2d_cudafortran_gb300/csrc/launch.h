@@ -111,6 +111,11 @@ struct TapeOut {
 // tape; tape.only writes just those.
 void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double> in, Field<double> out,
                        StepDt<double> sd, Ctl* ctl, const TapeOut& tape, cudaStream_t s);
+// The step with primitives kept beside the states (as the run's advance):
+// qmap maps the input's primitives (current, ghosts and corners included);
+// the output's go to qout.  Ghosts of the output are filled.
+void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, Field<double> in, Field<double> out,
+                        Field<double> qout, StepDt<double> sd, Ctl* ctl, cudaStream_t s);
 template <typename Real> void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in,
                                                Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
                                                cudaStream_t s);
