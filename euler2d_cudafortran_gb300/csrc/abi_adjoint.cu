@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <map>
 #include <string>
@@ -39,6 +40,7 @@ struct e2d_adjoint {
   // each), written by the forward sweeps and read by the reverse steps; null
   // when they could not be allocated (the reverse recomputes them)
   double* tapes = nullptr;
+  bool use_tape = true;  // E2D_NO_TAPE=1: the reverse recomputes (for comparisons)
   // primitives beside the two forward ping-pong states (the fast forward step
   // of e2d_advance: the step reads its input's and writes its output's);
   // null when they could not be allocated
@@ -137,7 +139,7 @@ int ensure(e2d_adjoint* a, int nsteps) {
   }
   A_CK(cudaMemsetAsync(a->pool, 0, (size_t)nstates * a->state_elems * sizeof(double), a->stream));
   const size_t tape_bytes = (size_t)2 * K * kTapePlanes * a->plane * sizeof(double);
-  if (cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
+  if (!a->use_tape || cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
     cudaGetLastError();
     a->tapes = nullptr;
   } else {
@@ -333,6 +335,7 @@ int e2d_adjoint_create(const e2d_params* p, e2d_adjoint** out) {
   a->plane = a->pitch * (size_t)(p->ny + 4);
   a->state_elems = 4 * a->plane;
   a->nparts = std::min(1024, p->ny);
+  if (const char* t = std::getenv("E2D_NO_TAPE")) a->use_tape = !(t[0] == '1');
   const size_t sb = a->state_elems * sizeof(double);
   if (cudaMalloc(&a->ub[0], sb) != cudaSuccess || cudaMalloc(&a->ub[1], sb) != cudaSuccess ||
       cudaMalloc(&a->ub[2], sb) != cudaSuccess ||
