@@ -119,15 +119,6 @@ template <> __device__ __forceinline__ double rabs<double>(double a) {
 }
 #endif
 
-// a*b rounded to nearest, as an instruction the compiler may not move out of
-// the branch that holds it (a multiplication is otherwise free to be
-// computed ahead of the test that makes it unnecessary).
-__device__ __forceinline__ double dmul_kept(double a, double b) {
-  double r;
-  asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
-  return r;
-}
-
 // max(a, b*c), the pressure floors of eos and the Riemann solvers (b a
 // density, c = smallp).  For double, when a is a positive normal number with
 // a >= 2^(ea-1023) >= 2^(eb+ec-2044) > b*c (ea, eb, ec the biased exponent
@@ -147,11 +138,7 @@ template <> __device__ __forceinline__ double floor_prod<double>(double a, doubl
   const bool dominant = (unsigned)(ha - 0x00100000) < 0x7fe00000u && (unsigned)hb < 0x7ff00000u &&
                         (unsigned)hc < 0x7ff00000u && (ha >> 20) >= (hb >> 20) + (hc >> 20) - 1021;
   if (dominant) return a;
-#if E2D_PFLOOR_EXP == 2
-  return Ops<double>::max(a, dmul_kept(b, c));
-#else
   return Ops<double>::max(a, b * c);
-#endif
 }
 #endif
 
@@ -227,45 +214,14 @@ __device__ __forceinline__ Real cell_invdt(const Hydro<Real>& h, const Real u[4]
 // dcen >= 0, dlim = 0 if dlft*drgt <= 0 else min(|dlft|,|drgt|), and the
 // slope dsgn*min(dlim,|dcen|).  st is 1 or 2; the products by st, 0.5 and
 // dsgn are exact scalings and sign flips.
-// dlim = (dlft*drgt <= 0) ? 0 : slop, slop = min(|dlft|, |drgt|).
-#ifndef E2D_LIMITER_SIGN
-#define E2D_LIMITER_SIGN 0
-#endif
+// dlim = (dlft*drgt <= 0) ? 0 : slop, slop = min(|dlft|, |drgt|).  (Deciding
+// the product's sign from signs and exponents on the integer pipe was
+// measured slower: the compiler predicates the rare IEEE fallback, and a
+// predicated FP64 instruction still takes its FP64 pipe slots.)
 template <typename Real>
 __device__ __forceinline__ Real limiter_dlim(Real dlft, Real drgt, Real slop) {
   return Ops<Real>::le0(dlft * drgt) ? Real(0.0) : slop;
 }
-#if !defined(E2D_FP64_NATIVE) && E2D_LIMITER_SIGN
-// For double, the product's sign is decided on the integer pipe when that is
-// exact: finite operands of opposite signs give a product <= 0 (-0 on
-// underflow); a zero operand makes slop +0, the result either way; normal
-// operands of the same sign whose biased exponents sum to at least 972 give
-// |dlft*drgt| >= 2^-1074, a positive product.  The rest (subnormal or tiny
-// same-sign pairs, infinities, NaN) form the IEEE product.
-template <>
-__device__ __forceinline__ double limiter_dlim<double>(double a, double b, double slop) {
-  const int ha = (int)(emul::bits(a) >> 32), hb = (int)(emul::bits(b) >> 32);
-  const unsigned ea = ((unsigned)ha >> 20) & 0x7ffu, eb = ((unsigned)hb >> 20) & 0x7ffu;
-  const bool zero = emul::bits(slop) == 0;
-  const bool opp = (ha ^ hb) < 0;
-  const bool fast = max(ea, eb) < 2047u && (opp || zero || (min(ea, eb) >= 1u && ea + eb >= 972u));
-  double r = (opp || zero) ? 0.0 : slop;
-#if E2D_LIMITER_SIGN == 2
-  if (__any_sync(__activemask(), !fast)) {
-    if (!fast) r = Ops<double>::le0(a * b) ? 0.0 : slop;
-  }
-#elif E2D_LIMITER_SIGN == 3
-  if (!fast) r = Ops<double>::le0(dmul_kept(a, b)) ? 0.0 : slop;
-#elif E2D_LIMITER_SIGN == 4
-  if (__any_sync(__activemask(), !fast)) {
-    if (!fast) r = Ops<double>::le0(dmul_kept(a, b)) ? 0.0 : slop;
-  }
-#else
-  if (!fast) r = Ops<double>::le0(a * b) ? 0.0 : slop;
-#endif
-  return r;
-}
-#endif
 
 template <typename Real>
 __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm) {
