@@ -453,19 +453,33 @@ def run_ours(a, dist):
     variants = None
     if dist.rank == 0 and not a.no_variants:
         variants = []
-        for (nx, prec, ver) in ((2048, 8, 1), (2048, 4, 0), (2048, 4, 1), (4096, 8, 0), (4096, 8, 1), (4096, 4, 0),
-                                (4096, 4, 1)):
+        # keep=False: implementationVersion 0 without the primitive arrays kept
+        # beside the states (E2D_KEEP_PRIMS=0: every step converts its box, the
+        # primitives never leave shared memory)
+        for (nx, prec, ver, keep) in ((2048, 8, 1, True), (2048, 8, 0, False), (2048, 4, 0, True), (2048, 4, 1, True),
+                                      (4096, 8, 0, True), (4096, 8, 1, True), (4096, 4, 0, True), (4096, 4, 1, True)):
             p = E.make_params(nx=nx, ny=nx, gamma0=1.4, cfl=0.8, implementation_version=ver,
                               riemann_solver=params.riemann_solver, precision=prec)
-            with E.HydroRun(p) as r3:
-                r3.init_implode()
-                ns = 20
-                r3.advance(0, 3, log=False)
-                r3.advance(3, ns, log=False)
-                r3.advance(3 + ns, ns, log=False)
-                vms = r3.last_advance_ms()
-            variants.append({"nx": nx, "precision": "FP64" if prec == 8 else "FP32", "implementationVersion": ver,
-                             "steps": ns, "mcells_per_s": round(nx * nx * ns / (vms * 1e-3) / 1e6, 2)})
+            old_keep = os.environ.get("E2D_KEEP_PRIMS")
+            os.environ["E2D_KEEP_PRIMS"] = "1" if keep else "0"
+            try:
+                with E.HydroRun(p) as r3:
+                    r3.init_implode()
+                    ns = 20
+                    r3.advance(0, 3, log=False)
+                    r3.advance(3, ns, log=False)
+                    r3.advance(3 + ns, ns, log=False)
+                    vms = r3.last_advance_ms()
+            finally:
+                if old_keep is None:
+                    os.environ.pop("E2D_KEEP_PRIMS", None)
+                else:
+                    os.environ["E2D_KEEP_PRIMS"] = old_keep
+            row = {"nx": nx, "precision": "FP64" if prec == 8 else "FP32", "implementationVersion": ver,
+                   "steps": ns, "mcells_per_s": round(nx * nx * ns / (vms * 1e-3) / 1e6, 2)}
+            if ver == 0:
+                row["primitives_kept"] = keep
+            variants.append(row)
 
     # FP32 against the FP64 oracle: the FP64 run is bitwise the oracle's, so
     # its state after `steps` steps stands for it

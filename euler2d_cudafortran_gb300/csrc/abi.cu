@@ -308,7 +308,11 @@ int e2d_create(const e2d_params* p, e2d_run** out) {
   for (int k = 0; k < nwork; ++k) cudaMemsetAsync(r->work[k], 0, sb, r->stream);
   cudaMemsetAsync(r->ctl, 0, sizeof(Ctl), r->stream);
   if (p->implementation_version == 0) {
-    if (cudaMalloc(&r->qprim[0], sb) != cudaSuccess || cudaMalloc(&r->qprim[1], sb) != cudaSuccess) {
+    // E2D_KEEP_PRIMS=0: no primitive arrays (every step converts its box;
+    // primitives never leave shared memory)
+    const char* kp = std::getenv("E2D_KEEP_PRIMS");
+    const bool keep = !(kp && kp[0] == '0');
+    if (keep && (cudaMalloc(&r->qprim[0], sb) != cudaSuccess || cudaMalloc(&r->qprim[1], sb) != cudaSuccess)) {
       cudaGetLastError();
       cudaFree(r->qprim[0]);
       r->qprim[0] = r->qprim[1] = nullptr;

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -290,7 +291,9 @@ int e2d_batch_create(const e2d_params* base, int nprob, const int* nx, const int
   cudaMemsetAsync(b->pool_u, 0, total * b->es, b->stream);
   cudaMemsetAsync(b->pool_u2, 0, total * b->es, b->stream);
   cudaMemsetAsync(b->ctls, 0, sizeof(Ctl) * (size_t)nprob, b->stream);
-  if (cudaMalloc(&b->pool_q, total * b->es) != cudaSuccess || cudaMalloc(&b->pool_q2, total * b->es) != cudaSuccess) {
+  const char* kp = std::getenv("E2D_KEEP_PRIMS");  // "0": no primitive arrays, as for a single run
+  if ((kp && kp[0] == '0') || cudaMalloc(&b->pool_q, total * b->es) != cudaSuccess ||
+      cudaMalloc(&b->pool_q2, total * b->es) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(b->pool_q);
     b->pool_q = b->pool_q2 = nullptr;

@@ -90,3 +90,24 @@ def test_percall_steps_see_an_uploaded_state(e2d, prec):
         b.make_boundaries(0)
         ub = b.get_state(0)
     assert np.array_equal(ua, ub)
+
+
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+def test_kept_primitives_change_no_bit(e2d, monkeypatch, prec):
+    """implementationVersion 0 keeps the primitives of its states beside them
+    (each step writes its output's); with E2D_KEEP_PRIMS=0 every step
+    converts its box instead.  Both give the same states and dt."""
+    p = _params(e2d, 0, prec)
+    runs = []
+    for keep in ("1", "0"):
+        monkeypatch.setenv("E2D_KEEP_PRIMS", keep)
+        with e2d.HydroRun(p) as r:
+            r.init_implode()
+            dts = r.advance(0, 9)
+            for n in range(9, 13):
+                dts = np.append(dts, r.compute_dt(n % 2))
+                r.godunov_unsplit(n, dts[-1])
+            r.make_boundaries(1)
+            runs.append((r.get_state(1), dts))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
