@@ -11,15 +11,26 @@
 #include <algorithm>
 
 #include "batch.h"
+#include "sync.cuh"
 #include "tile.cuh"
 
 namespace e2d {
 
 namespace {
 
+// 16-byte asynchronous copy global -> shared; the bytes past src_bytes (0, 8
+// or 16) are zero-filled, what TMA zero fill gives outside the array.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
 // SQ: every problem of the launch has dx == dy (the shared face source term
 // of tile_compute).  QIN: the boxes are read from the primitives kept beside
 // the states, and the update writes those of the new state (tile_compute).
+// A CTA walks the flattened tiles with a fixed stride; the box of its next
+// tile is copied asynchronously (cp.async) as soon as the face phase of the
+// current one ends -- into the primitives region with QIN, else into the
+// slope region -- so it lands while the update phase runs.
 template <typename Real, class C, int MINB, bool SQ, bool QIN>
 __global__ void __launch_bounds__(C::NT, MINB)
     k_batch_step(const BatchProb<Real>* __restrict__ probs, int nprob, int total_tiles, int parity, int rd, int wr,
@@ -31,48 +42,76 @@ __global__ void __launch_bounds__(C::NT, MINB)
   Real* red = reinterpret_cast<Real*>(tail + 16);
   Real* sdt = red + 32;
   __shared__ Hydro<Real> sh;
-  __shared__ int sp, sid, stile;
+  __shared__ int cur[3], nxt[3];  // problem (work-list order), problem index, tile within the problem
   const int tid = threadIdx.x;
+  Real* const dreg = QIN ? base + C::q_off : base + C::d_off;  // where a prefetched box lands
+  static_assert(8ull * C::RY * C::RX >= 4ull * C::BYs * C::BXs, "the next box fits in the slope region");
+  static_assert((C::d_off * sizeof(Real)) % 16 == 0 && (C::BXs * sizeof(Real)) % 16 == 0,
+                "16-byte aligned copy destinations");
 
-  for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+  auto lookup = [&](int t, int* info) {  // thread 0
+    int lo = 0, hi = nprob - 1;  // last problem with tile_begin <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].tile_begin <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    info[0] = lo;
+    info[1] = probs[lo].id;
+    info[2] = t - probs[lo].tile_begin;
+  };
+  auto issue = [&](const int* info, Real* dst) {  // every thread: its part of the box of tile `info`
+    const BatchProb<Real>& P = probs[info[0]];
+    const int i0 = GW + (info[2] % P.ntx) * C::TX, j0 = GW + (info[2] / P.ntx) * C::TY;
+    const Real* b = QIN ? (parity ? P.q2 : P.q) : (parity ? P.u2 : P.u);
+    const int isize = P.h.isize, jsize = P.h.jsize;
+    constexpr int CH = 16 / (int)sizeof(Real), NCH = C::BXs / CH;
+    static_assert(C::BXs % CH == 0, "box rows of whole 16-byte chunks");
+    for (int k = tid; k < 4 * C::BYs * NCH; k += C::NT) {
+      const int v = k / (C::BYs * NCH), rem = k - v * (C::BYs * NCH);
+      const int y = rem / NCH, c = rem - y * NCH;
+      const int gi = i0 - GW + c * CH, gj = j0 - GW + y;
+      const int n = gj < jsize ? max(0, min(isize - gi, CH)) : 0;
+      const Real* src = n ? b + (long long)v * P.plane + (long long)gj * P.pitch + gi : b;
+      cp_async16(smem_u32(dst + (v * C::BYs + y) * C::BXs + c * CH), src, n * (int)sizeof(Real));
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  int t = blockIdx.x;
+  if (t >= total_tiles) return;
+  if (tid == 0) lookup(t, cur);
+  __syncthreads();
+  issue(cur, base + C::q_off);
+  bool first = true;
+  for (; t < total_tiles; t += gridDim.x) {
     if (tid == 0) {
-      int lo = 0, hi = nprob - 1;  // last problem with tile_begin <= t
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (probs[mid].tile_begin <= t) lo = mid;
-        else hi = mid - 1;
-      }
-      sp = lo;
-      sid = probs[lo].id;
-      stile = t - probs[lo].tile_begin;
-      sh = probs[lo].h;
+      sh = probs[cur[0]].h;
       *face_counter = 0;
-      const Real dt0 = dt_src ? dt_src[sid] : sh.cfl / *inv_slot<Real>(&ctls[sid], rd);
+      const Real dt0 = dt_src ? dt_src[cur[1]] : sh.cfl / *inv_slot<Real>(&ctls[cur[1]], rd);
       sdt[0] = dt0;
       sdt[1] = dt0 / sh.dx;
       sdt[2] = dt0 / sh.dy;
     }
-    __syncthreads();
-    const int p = sp, id = sid;
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();  // every thread's copies, the problem's parameters and dt
+    const int p = cur[0], id = cur[1], stile = cur[2];
     const BatchProb<Real>& P = probs[p];
-    const int tx = stile % P.ntx, ty = stile / P.ntx;
-    const int i0 = GW + tx * C::TX, j0 = GW + ty * C::TY;
+    const int i0 = GW + (stile % P.ntx) * C::TX, j0 = GW + (stile / P.ntx) * C::TY;
     Field<Real> in{parity ? P.u2 : P.u, P.pitch, P.plane};
     Field<Real> out{parity ? P.u : P.u2, P.pitch, P.plane};
-    const Field<Real> box{QIN ? (parity ? P.q2 : P.q) : in.p, P.pitch, P.plane};
     const Field<Real> qout{QIN ? (parity ? P.q : P.q2) : out.p, P.pitch, P.plane};
-    // conservative (or primitive) box, zero outside the array (what TMA zero
-    // fill gives)
-    Real* sq = base + C::q_off;
-    for (int k = tid; k < 4 * C::BYs * C::BXs; k += C::NT) {
-      const int v = k / (C::BYs * C::BXs), rem = k - v * (C::BYs * C::BXs);
-      const int y = rem / C::BXs, x = rem - y * C::BXs;
-      const int gi = i0 - GW + x, gj = j0 - GW + y;
-      sq[k] = (gi < sh.isize && gj < sh.jsize) ? box.at(v, gj, gi) : Real(0);
-    }
-    __syncthreads();
+    const int next = t + gridDim.x;
+    auto prefetch = [&]() {  // every thread, right after the face phase
+      if (next < total_tiles) {
+        if (tid == 0) lookup(next, nxt);
+        __syncthreads();
+        issue(nxt, dreg);
+      }
+    };
     Real m = tile_compute<Real, C, SQ, QIN>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1], sdt[2],
-                                            true, wr >= 0, &ctls[id].health);
+                                            true, wr >= 0, &ctls[id].health, (QIN || first) ? nullptr : dreg,
+                                            prefetch);
     if (tid == 0) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];
@@ -80,11 +119,17 @@ __global__ void __launch_bounds__(C::NT, MINB)
         if (!isfinite(sdt[0])) atomicOr(&ctls[id].health, 1u);
       }
       if (wr >= 0) {
-        m = fmax(m, *inv_slot<Real>(&ctls[id], rd));
+        m = Ops<Real>::max(m, *inv_slot<Real>(&ctls[id], rd));
         atomic_max_slot_ptr<Real>(inv_slot<Real>(&ctls[id], wr), m);
       }
     }
-    __syncthreads();  // shared memory is reused by the next tile
+    __syncthreads();  // the tile's shared data consumed
+    if (tid == 0) {
+      cur[0] = nxt[0];
+      cur[1] = nxt[1];
+      cur[2] = nxt[2];
+    }
+    first = false;
   }
 }
 
