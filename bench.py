@@ -538,7 +538,10 @@ def run_ours(a, dist):
             "cpu_baseline": cpu,
             "cpu_baseline_multicore": cpu_mc,
             "clocks": clk,
-            "gpu_launches": a.steps + 1 if a.version == 0 else 4 * a.steps,
+            # timed advance call: make_boundaries, (version 0 with kept primitives) the
+            # primitives of both buffers, then the steps
+            "gpu_launches": (a.steps + 1 + (0 if os.environ.get("E2D_KEEP_PRIMS") == "0" else 2)
+                             if a.version == 0 else 4 * a.steps),
             "health_flags": health,
             "variants": variants,
             "fp32_error_vs_fp64_oracle": fp32_error,
