@@ -253,6 +253,20 @@ __global__ void k_trace_v1(Hydro<Real> h, Field<Real> q, StepDt<Real> sd, Ctl* c
   load4(q, j, i, qc); load4(q, j, i + 1, qe); load4(q, j, i - 1, qw); load4(q, j + 1, i, qn); load4(q, j - 1, i, qs);
   slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
   trace_sources(h, qc, dqx, dqy, s);
+  // FP64 with dtdx == dtdy: the source term (s*dtd)*0.5 is the same for the
+  // four faces (+0.8 %; the FP32 build, not bound by its FP pipes, is left as it is)
+  if constexpr (sizeof(Real) == 8) {
+    if (h.dx == h.dy) {
+      Real sh[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sh[v] = Ops<Real>::half(s[v] * dtdx);
+      trace_face<Real, false, true>(h, qc, dqx, sh, dtdx, f); store4(qxm, j, i, f);
+      trace_face<Real, true, true>(h, qc, dqx, sh, dtdx, f);  store4(qxp, j, i, f);
+      trace_face<Real, false, true>(h, qc, dqy, sh, dtdy, f); store4(qym, j, i, f);
+      trace_face<Real, true, true>(h, qc, dqy, sh, dtdy, f);  store4(qyp, j, i, f);
+      return;
+    }
+  }
   trace_face<Real, false>(h, qc, dqx, s, dtdx, f); store4(qxm, j, i, f);
   trace_face<Real, true>(h, qc, dqx, s, dtdx, f);  store4(qxp, j, i, f);
   trace_face<Real, false>(h, qc, dqy, s, dtdy, f); store4(qym, j, i, f);
