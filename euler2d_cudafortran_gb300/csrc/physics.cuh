@@ -355,9 +355,6 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
 }
 
 // riemann_2d_hllc, serial_ref/m_utils.f90:534-644 (rcsum, unused there, is not formed).
-#ifndef E2D_HLLC_ONESTAR
-#define E2D_HLLC_ONESTAR 0
-#endif
 template <typename Real>
 __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real qleft[4],
                                              const Real qright[4], Real flux[4]) {
@@ -388,22 +385,6 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real ustar = O::div(((rcr * ur) + (rcl * ul)) + (ptotl - ptotr), rcr + rcl);
   const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
   Real ro, uo, ptoto, etoto;
-#if E2D_HLLC_ONESTAR
-  // The side first (SL > 0: left state; ustar > 0: left star; SR > 0: right
-  // star; else right state), then one star state from its values.
-  const bool slpos = O::gt0(SL), uspos = O::gt0(ustar);
-  const bool lside = slpos || uspos;
-  const Real SK = lside ? SL : SR, rK = lside ? rl : rr, uK = lside ? ul : ur;
-  const Real eK = lside ? etotl : etotr, pK = lside ? ptotl : ptotr;
-  if (!slpos && (uspos || O::gt0(SR))) {
-    const Real dS = SK - uK, den = SK - ustar;
-    ro = O::div(rK * dS, den);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div((((dS * eK) - (pK * uK)) + (ptotstar * ustar)), den);
-  } else {
-    ro = rK; uo = uK; ptoto = pK; etoto = eK;
-  }
-#else
   if (O::gt0(SL)) {
     ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
   } else if (O::gt0(ustar)) {
@@ -417,7 +398,6 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   } else {
     ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
   }
-#endif
   flux[ID] = ro * uo;
   flux[IU] = ((ro * uo) * uo) + ptoto;
   flux[IP] = (etoto + ptoto) * uo;
