@@ -79,25 +79,9 @@ Field<double> state(const e2d_adjoint* a, int k) {
 }
 Field<double> ubf(const e2d_adjoint* a, int k) { return Field<double>{a->ub[k], (int)a->pitch, (long long)a->plane}; }
 
-// Planes of one tape: q 4, dq 8, s 4, x and y face records HR_N each, and
-// the two planes of 32-bit face flags in one plane of doubles.
-constexpr int kTapePlanes = 4 + 8 + 4 + 2 * HR_N + 1;
-
 // The tape of segment state j of set `set`.
 TapeOut tape_of(const e2d_adjoint* a, int set, int j, bool only = false) {
-  TapeOut t;
-  double* b = a->tapes + (size_t)(set * a->kseg + j) * kTapePlanes * a->plane;
-  t.q = b;
-  t.dq = b + 4 * a->plane;
-  t.s = b + 12 * a->plane;
-  t.fx = b + 16 * a->plane;
-  t.fy = t.fx + HR_N * a->plane;
-  t.flx = reinterpret_cast<unsigned*>(t.fy + HR_N * a->plane);
-  t.fly = t.flx + a->plane;
-  t.pitch = (int)a->pitch;
-  t.plane = (long long)a->plane;
-  t.only = only ? 1 : 0;
-  return t;
+  return tape_at(a->tapes, set * a->kseg + j, (long long)a->plane, (int)a->pitch, only);
 }
 
 Field<double> qpf(const e2d_adjoint* a, int k) {

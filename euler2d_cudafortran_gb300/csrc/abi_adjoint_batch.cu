@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <map>
 #include <numeric>
@@ -47,6 +48,15 @@ struct e2d_adjoint_batch {
   AdjProb* d_probs = nullptr;          // by problem index
   BatchProb<double>* d_fwd = nullptr;  // forward ping-pong, work-list order
   BatchProb<double>* d_seg = nullptr;  // [2][K - 1][nprob]: segment set, state j -> j + 1
+  // The tape (one set of K segment states per problem, written by the
+  // forward sweep's last segment and by each recomputation, read by the
+  // reverse steps), when it fits in half the free memory and E2D_NO_TAPE is
+  // not 1; the recomputation then follows each segment's reverse sweep
+  // instead of overlapping it.
+  double* tapes = nullptr;
+  bool use_tape = true;
+  BatchProb<double>* d_fwdtape = nullptr;  // [K][nprob]: forward steps of the last segment, with tapes
+  BatchProb<double>* d_segonly = nullptr;  // [2][nprob]: the tape-only pass of a segment's last state
   int fwd_tiles = 0, fwd_grid = 0, rev_tiles = 0, nparts = 64;
   bool square = false;  // every problem has dx == dy
   Ctl* ctls = nullptr;
@@ -87,6 +97,11 @@ void free_slab(e2d_adjoint_batch* b) {
   cudaFree(b->d_probs);
   cudaFree(b->d_fwd);
   cudaFree(b->d_seg);
+  cudaFree(b->tapes);
+  cudaFree(b->d_fwdtape);
+  cudaFree(b->d_segonly);
+  b->tapes = nullptr;
+  b->d_fwdtape = b->d_segonly = nullptr;
   cudaFree(b->dt_log);
   cudaFree(b->inv_log);
   cudaFree(b->dtbar_log);
@@ -141,6 +156,28 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
     return abfail(E2D_ERR_OOM, "cudaMalloc of the batched adjoint checkpoints failed");
   }
   AB_CK(cudaMemsetAsync(b->slab, 0, total * sizeof(double), b->stream));
+  // the tape: K tapes per problem, if they take at most half the free memory
+  std::vector<size_t> tape_off(b->nprob);
+  size_t tape_total = 0;
+  for (int p = 0; p < b->nprob; ++p) {
+    tape_off[p] = tape_total;
+    tape_total += (size_t)K * kTapePlanes * b->plane[p];
+  }
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  if (b->use_tape && tape_total * sizeof(double) <= free_b / 2 &&
+      cudaMalloc(&b->tapes, tape_total * sizeof(double)) == cudaSuccess &&
+      cudaMalloc(&b->d_fwdtape, sizeof(BatchProb<double>) * b->nprob * K) == cudaSuccess &&
+      cudaMalloc(&b->d_segonly, sizeof(BatchProb<double>) * b->nprob * 2) == cudaSuccess) {
+    AB_CK(cudaMemsetAsync(b->tapes, 0, tape_total * sizeof(double), b->stream));  // unwritten cells read zeros
+  } else {
+    cudaGetLastError();
+    cudaFree(b->tapes);
+    cudaFree(b->d_fwdtape);
+    cudaFree(b->d_segonly);
+    b->tapes = nullptr;
+    b->d_fwdtape = b->d_segonly = nullptr;
+  }
   // reverse tiles by problem index
   int rtx, rty;
   rev_tile_shape(&rtx, &rty);
@@ -158,6 +195,7 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
     P.nty = (b->params[p].ny + rty - 1) / rty;
     P.tile_begin = t;
     P.grad_off = b->grad_off[p];
+    P.tape_base = b->tapes ? b->tapes + tape_off[p] : nullptr;
     t += P.ntx * P.nty;
   }
   b->rev_tiles = t;
@@ -170,7 +208,7 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
     return (long long)b->params[x].nx * b->params[x].ny > (long long)b->params[y].nx * b->params[y].ny;
   });
   const size_t nseg_arr = (size_t)b->nprob * std::max(1, K - 1);
-  std::vector<BatchProb<double>> fw(b->nprob), sg(2 * nseg_arr);
+  std::vector<BatchProb<double>> fw(b->nprob), sg(2 * nseg_arr), fwt((size_t)K * b->nprob), so(2 * b->nprob);
   int ft = 0;
   for (int k = 0; k < b->nprob; ++k) {
     const int p = order[k];
@@ -185,13 +223,27 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
     F.tile_begin = ft;
     F.id = p;
     ft += F.ntx * F.nty;
-    for (int set = 0; set < 2; ++set)
+    const auto tape = [&](int j, bool only) {
+      return b->tapes ? tape_at(b->tapes + tape_off[p], j, (long long)b->plane[p], (int)b->pitch[p], only)
+                      : TapeOut();
+    };
+    for (int set = 0; set < 2; ++set) {
       for (int j = 0; j + 1 < K; ++j) {
         BatchProb<double>& S = sg[set * nseg_arr + (size_t)j * b->nprob + k];
         S = F;
         S.u = ap[p].base + (size_t)(seg_base(b) + set * K + j) * b->se[p];
         S.u2 = ap[p].base + (size_t)(seg_base(b) + set * K + j + 1) * b->se[p];
+        S.tape = tape(j, false);
       }
+      BatchProb<double>& O = so[(size_t)set * b->nprob + k];  // state K - 1 of the set, read at parity 0
+      O = F;
+      O.u = O.u2 = ap[p].base + (size_t)(seg_base(b) + set * K + (K - 1)) * b->se[p];
+      O.tape = tape(K - 1, true);
+    }
+    for (int j = 0; j < K; ++j) {
+      fwt[(size_t)j * b->nprob + k] = F;
+      fwt[(size_t)j * b->nprob + k].tape = tape(j, false);
+    }
   }
   b->fwd_tiles = ft;
   b->square = std::all_of(fw.begin(), fw.end(), [](const BatchProb<double>& F) { return F.h.dx == F.h.dy; });
@@ -203,6 +255,12 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
                         b->stream));
   AB_CK(cudaMemcpyAsync(b->d_seg, sg.data(), sizeof(BatchProb<double>) * sg.size(), cudaMemcpyHostToDevice,
                         b->stream));
+  if (b->tapes) {
+    AB_CK(cudaMemcpyAsync(b->d_fwdtape, fwt.data(), sizeof(BatchProb<double>) * fwt.size(), cudaMemcpyHostToDevice,
+                          b->stream));
+    AB_CK(cudaMemcpyAsync(b->d_segonly, so.data(), sizeof(BatchProb<double>) * so.size(), cudaMemcpyHostToDevice,
+                          b->stream));
+  }
   AB_CK(cudaStreamSynchronize(b->stream));
   b->cap_steps = nsteps;
   return E2D_OK;
@@ -250,13 +308,15 @@ void enqueue_forward(e2d_adjoint_batch* b, int nsteps, double xc, double yc, dou
       if (k >= last * K) launch_batch_copy(B, kPing + (k & 1), seg_base(b) + (last & 1) * K + (k - last * K), s);
       else if (k % K == 0) launch_batch_copy(B, kPing + (k & 1), kChk + k / K, s);
     }
-    BatchLaunch<double> L = step_launch(b, b->d_fwd);
+    const bool taping = adjoint && b->tapes && k >= last * K;
+    BatchLaunch<double> L = step_launch(b, taping ? b->d_fwdtape + (size_t)(k - last * K) * b->nprob : b->d_fwd);
     L.parity = k & 1;
     L.rd = k & 1;
     L.wr = L.rd ^ 1;
     L.dt_log = b->dt_log + (size_t)k * b->nprob;
     L.inv_log = b->inv_log + (size_t)k * b->nprob;
-    launch_batch_step<double>(0, L, s);
+    if (taping) launch_batch_step_tape(L, s);
+    else launch_batch_step<double>(0, L, s);
   }
   cudaMemsetAsync(b->J, 0, sizeof(double) * b->nprob, s);
   launch_batch_objective(B, kPing + (nsteps & 1), xc, yc, sig, adjoint ? ub_base(b) : -1, s);
@@ -273,7 +333,13 @@ void enqueue_recompute(e2d_adjoint_batch* b, int sg, int set, int nsteps, cudaSt
   for (int m = k0; m < k1 - 1; ++m) {
     BatchLaunch<double> L = step_launch(b, b->d_seg + set * nseg_arr + (size_t)(m - k0) * b->nprob);
     L.dt_src = b->dt_log + (size_t)m * b->nprob;
-    launch_batch_step<double>(0, L, s);
+    if (b->tapes) launch_batch_step_tape(L, s);
+    else launch_batch_step<double>(0, L, s);
+  }
+  if (b->tapes) {  // the segment's last state has no step here: its tape alone
+    BatchLaunch<double> L = step_launch(b, b->d_segonly + (size_t)set * b->nprob);
+    L.dt_src = b->dt_log + (size_t)(k1 - 1) * b->nprob;
+    launch_batch_step_tape(L, s);
   }
 }
 
@@ -290,7 +356,7 @@ void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
   // the last segment's states were kept by the forward sweep
   for (int sg = last; sg >= 0; --sg) {
     const int set = sg & 1, k0 = sg * K, k1 = std::min(k0 + K, nsteps), sb = seg_base(b) + set * K;
-    if (sg > 0) {
+    if (sg > 0 && !b->tapes) {
       cudaEventRecord(b->fork, s);
       cudaStreamWaitEvent(s2, b->fork, 0);
       enqueue_recompute(b, sg - 1, set ^ 1, nsteps, s2);
@@ -298,14 +364,18 @@ void enqueue_reverse(e2d_adjoint_batch* b, int nsteps, int dt_mode) {
     }
     for (int m = k1 - 1; m >= k0; --m) {
       const int nxt = (cur + 1) % 3, zro = (cur + 2) % 3;
-      launch_batch_step_rev(B, sb + (m - k0), ub + cur, ub + nxt, m > 0 ? ub + zro : -1, m, s);
+      launch_batch_step_rev(B, sb + (m - k0), ub + cur, ub + nxt, m > 0 ? ub + zro : -1, m, s,
+                            b->tapes ? m - k0 : -1);
       if (dt_mode == 1) {
         launch_batch_argmax(B, sb + (m - k0), m, s);
         launch_batch_dt_route(B, sb + (m - k0), ub + nxt, m, nsteps, s);
       }
       cur = nxt;
     }
-    if (sg > 0) cudaStreamWaitEvent(s, b->join, 0);
+    if (sg > 0) {
+      if (b->tapes) enqueue_recompute(b, sg - 1, set ^ 1, nsteps, s);  // the one tape set is free now
+      else cudaStreamWaitEvent(s, b->join, 0);
+    }
   }
   launch_batch_extract(B, ub + cur, b->grad, s);
 }
@@ -380,6 +450,7 @@ int e2d_adjoint_batch_create(const e2d_params* base, int nprob, const int* nx, c
     return abfail(E2D_ERR_NO_DEVICE, "no CUDA device");
   }
   e2d_adjoint_batch* b = new e2d_adjoint_batch;
+  if (const char* t = std::getenv("E2D_NO_TAPE")) b->use_tape = !(t[0] == '1');
   b->nprob = nprob;
   cudaGetDevice(&b->device);
   size_t u0_total = 0;

@@ -15,6 +15,7 @@ struct AdjProb {
   long long plane;
   int ntx, nty, tile_begin;  // 32 x 7 tiles; this problem's first tile in the flattened list
   long long grad_off;        // this problem's nx*ny gradient in the packed output
+  double* tape_base;         // K tapes (kTapePlanes planes each) of the segment states; null: none
 };
 
 // The device-side view of a batched adjoint; logs are step-major
@@ -33,7 +34,9 @@ struct AdjBatch {
 
 int batch_step_rev_setup();
 int rev_tile_shape(int* tx, int* ty);
-void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s);
+// tape_j >= 0: every problem's reverse reads its tape tape_j (AdjProb::tape_base).
+void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s,
+                           int tape_j = -1);
 void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s);
 void launch_batch_dt_route(const AdjBatch& B, int un, int ub_out, int m, int nsteps, cudaStream_t s);
 // J[p] += sum rho^2 w of buffer un; seed_ub >= 0: that buffer = dJ/dU on the interior.

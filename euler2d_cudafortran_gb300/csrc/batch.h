@@ -16,6 +16,7 @@ struct BatchProb {
   int ntx, nty;    // tiles of the chosen shape
   int tile_begin;  // first index of this problem in the flattened tile list
   int id;          // problem index (its control block and dt-log column)
+  TapeOut tape;    // (FP64 adjoint) where a taping step leaves its input's forward values
 };
 
 template <typename Real>
@@ -29,6 +30,10 @@ struct BatchLaunch {
   bool square = false;           // every problem has dx == dy (selects the kernel that shares face sources)
   bool qin = false;              // the boxes are read from q/q2 (current), and the step writes the next ones
 };
+
+// (FP64, 32 x 15 tiles, conservative boxes) the step that also writes each
+// problem's tape (BatchProb::tape; tape.only: just the tape).
+void launch_batch_step_tape(const BatchLaunch<double>& L, cudaStream_t s);
 
 // Tile shapes: variant 0 = 32 x 15 cells (256 threads), 1 = 32 x 7 (128 threads).
 template <typename Real> int batch_tile_shape(int variant, int* tx, int* ty, int* nt);

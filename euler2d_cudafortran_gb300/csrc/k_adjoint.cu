@@ -545,10 +545,10 @@ __device__ __forceinline__ Field<double> afield(const AdjProb& P, int k) {
 
 // Reverse step m of every problem: one CTA per 32 x 7 tile of the flattened
 // tile list (problem p owns tiles [tile_begin, tile_begin + ntx * nty)).
-template <bool SQ>
+template <bool SQ, bool TAPE>
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_batch_step_rev(const AdjProb* __restrict__ probs, int nprob, const double* dt_log, double* dtbar_log, int un,
-                     int ub_in, int ub_out, int ub_zero, int m) {
+                     int ub_in, int ub_out, int ub_zero, int m, int tape_j) {
   extern __shared__ double sm[];
   __shared__ Hydro<double> sh;
   __shared__ int sp;
@@ -567,9 +567,10 @@ __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
   const AdjProb& P = probs[sp];
   const int tile = t - P.tile_begin;
   const long long row = (long long)m * nprob + sp;
-  step_rev_tile<SQ>(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out),
-                ub_zero >= 0 ? afield(P, ub_zero) : Field<double>{nullptr, 0, 0}, dt_log[row], dtbar_log + row,
-                tile % P.ntx, tile / P.ntx, sm);
+  const TapeOut tp = TAPE ? tape_at(P.tape_base, tape_j, P.plane, P.pitch, false) : TapeOut();
+  step_rev_tile<SQ, TAPE>(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out),
+                          ub_zero >= 0 ? afield(P, ub_zero) : Field<double>{nullptr, 0, 0}, dt_log[row],
+                          dtbar_log + row, tile % P.ntx, tile / P.ntx, sm, tp);
 }
 
 __global__ void k_batch_argmax(const AdjProb* __restrict__ probs, int nprob, const double* inv_log, int un, int m,
@@ -678,12 +679,11 @@ void launch_objective(const Hydro<double>& h, Field<double> u, double xc, double
 }
 
 int batch_step_rev_setup() {
-  return cudaFuncSetAttribute(k_batch_step_rev<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)SMEM_BYTES) == cudaSuccess &&
-                 cudaFuncSetAttribute(k_batch_step_rev<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)SMEM_BYTES) == cudaSuccess
-             ? 0
-             : -1;
+  bool ok = true;
+  for (auto f : {k_batch_step_rev<false, false>, k_batch_step_rev<true, false>, k_batch_step_rev<false, true>,
+                 k_batch_step_rev<true, true>})
+    ok = ok && cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) == cudaSuccess;
+  return ok ? 0 : -1;
 }
 
 int rev_tile_shape(int* tx, int* ty) {
@@ -692,13 +692,19 @@ int rev_tile_shape(int* tx, int* ty) {
   return 0;
 }
 
-void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s) {
-  if (B.square)
-    k_batch_step_rev<true><<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in,
-                                                                  ub_out, ub_zero, m);
-  else
-    k_batch_step_rev<false><<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in,
-                                                                   ub_out, ub_zero, m);
+void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int ub_zero, int m, cudaStream_t s,
+                           int tape_j) {
+  const auto args = [&](auto kern) {
+    kern<<<B.total_tiles, ANT, SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in, ub_out, ub_zero,
+                                                m, tape_j);
+  };
+  if (tape_j >= 0) {
+    if (B.square) args(k_batch_step_rev<true, true>);
+    else args(k_batch_step_rev<false, true>);
+  } else {
+    if (B.square) args(k_batch_step_rev<true, false>);
+    else args(k_batch_step_rev<false, false>);
+  }
 }
 
 void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s) {

@@ -31,7 +31,8 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int sr
 // tile is copied asynchronously (cp.async) as soon as the face phase of the
 // current one ends -- into the primitives region with QIN, else into the
 // slope region -- so it lands while the update phase runs.
-template <typename Real, class C, int MINB, bool SQ, bool QIN>
+// TAPE (FP64, !QIN): the step also writes each problem's tape (BatchProb::tape).
+template <typename Real, class C, int MINB, bool SQ, bool QIN, bool TAPE = false>
 __global__ void __launch_bounds__(C::NT, MINB)
     k_batch_step(const BatchProb<Real>* __restrict__ probs, int nprob, int total_tiles, int parity, int rd, int wr,
                  Ctl* ctls, Real* dt_log, const Real* dt_src, Real* inv_log) {
@@ -109,10 +110,11 @@ __global__ void __launch_bounds__(C::NT, MINB)
         issue(nxt, dreg);
       }
     };
-    Real m = tile_compute<Real, C, SQ, QIN>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1], sdt[2],
-                                            true, wr >= 0, &ctls[id].health, (QIN || first) ? nullptr : dreg,
-                                            prefetch);
-    if (tid == 0) {
+    const bool only = TAPE && P.tape.only;  // a tape-only pass: no update, no dt
+    Real m = tile_compute<Real, C, SQ, QIN, TAPE>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1],
+                                                  sdt[2], true, wr >= 0 && !only, &ctls[id].health,
+                                                  (QIN || first) ? nullptr : dreg, prefetch, &P.tape);
+    if (tid == 0 && !only) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];
         if (inv_log) inv_log[id] = *inv_slot<Real>(&ctls[id], rd);
@@ -176,6 +178,28 @@ template <typename Real> using V32x15 = Variant<Real, TileCfg<Real, 32, 15, 256>
 template <typename Real> using V32x7 = Variant<Real, TileCfg<Real, 32, 7, 128>, (sizeof(Real) == 8 ? 4 : 6)>;
 
 }  // namespace
+
+void launch_batch_step_tape(const BatchLaunch<double>& L, cudaStream_t s) {
+  using C = TileCfg<double, 32, 15, 256>;
+  static bool attrs = false;
+  if (!attrs) {  // dynamic shared memory and carveout, as for the other instantiations
+    cudaFuncSetAttribute(k_batch_step<double, C, 2, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)C::bytes);
+    cudaFuncSetAttribute(k_batch_step<double, C, 2, false, false, true>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);
+    cudaFuncSetAttribute(k_batch_step<double, C, 2, true, false, true>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_batch_step<double, C, 2, false, false, true>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    attrs = true;
+  }
+  if (L.square)
+    k_batch_step<double, C, 2, true, false, true><<<L.grid, C::NT, C::bytes, s>>>(
+        L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+  else
+    k_batch_step<double, C, 2, false, false, true><<<L.grid, C::NT, C::bytes, s>>>(
+        L.probs, L.nprob, L.total_tiles, L.parity, L.rd, L.wr, L.ctls, L.dt_log, L.dt_src, L.inv_log);
+}
 
 template <typename Real>
 int batch_tile_shape(int variant, int* tx, int* ty, int* nt) {

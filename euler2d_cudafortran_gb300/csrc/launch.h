@@ -107,6 +107,28 @@ struct TapeOut {
   }
 };
 
+// Planes of one tape: q 4, dq 8, s 4, x and y face records HR_N each, and
+// the two planes of 32-bit face flags in one plane of doubles.
+constexpr int kTapePlanes = 4 + 8 + 4 + 2 * HR_N + 1;
+
+// Tape j of a run of tapes at `base` (kTapePlanes planes each) of a state
+// with `plane` elements per plane and row pitch `pitch`.
+__host__ __device__ inline TapeOut tape_at(double* base, int j, long long plane, int pitch, bool only) {
+  TapeOut t;
+  double* b = base + (long long)j * kTapePlanes * plane;
+  t.q = b;
+  t.dq = b + 4 * plane;
+  t.s = b + 12 * plane;
+  t.fx = b + 16 * plane;
+  t.fy = t.fx + HR_N * plane;
+  t.flx = reinterpret_cast<unsigned*>(t.fy + HR_N * plane);
+  t.fly = t.flx + plane;
+  t.pitch = pitch;
+  t.plane = plane;
+  t.only = only ? 1 : 0;
+  return t;
+}
+
 // The adjoint's forward step: also writes its input's forward values to the
 // tape; tape.only writes just those.
 void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double> in, Field<double> out,

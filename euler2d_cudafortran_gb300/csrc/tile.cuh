@@ -250,10 +250,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
   }
   __syncthreads();
+  after_faces();
   if constexpr (TAPE) {
     if (tape->only) return Real(0);
   }
-  after_faces();
 
   // ---- updateHydro + ghost copies + next-step CFL maximum
   Real m = Real(0);

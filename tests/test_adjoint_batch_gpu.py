@@ -87,3 +87,21 @@ def test_batch_adjoint_uploaded_state(e2d, oracle):
         Js, gs, _ = A.gradient(n, u0, dt_mode=1)
     assert abs(J[1] - Js) <= 1e-13 * abs(Js)
     assert rel_l1(grads[1], gs) <= 1e-11
+
+
+def test_batch_tape_gives_the_recomputed_gradient(e2d, monkeypatch):
+    """With the tape (written by the recomputation, the recomputation then
+    following each segment's reverse sweep) and without it (E2D_NO_TAPE=1:
+    the reverse recomputes, the recomputation overlaps it), the gradients
+    agree to round-off."""
+    n = 23  # K = 5: a ragged last segment, four recomputed segments
+    with make_batch(e2d) as b:
+        J1, g1, d1 = b.gradient(n, dt_mode=1)
+    monkeypatch.setenv("E2D_NO_TAPE", "1")
+    with make_batch(e2d) as b:
+        J2, g2, d2 = b.gradient(n, dt_mode=1)
+    assert np.array_equal(d1, d2)
+    for k in range(len(SIZES)):
+        assert abs(J1[k] - J2[k]) <= 1e-13 * abs(J2[k])
+        assert np.any(g1[k] != 0.0)
+        assert rel_l1(g1[k], g2[k]) <= 1e-12, (k, rel_l1(g1[k], g2[k]))
