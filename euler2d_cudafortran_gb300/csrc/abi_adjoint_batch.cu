@@ -43,6 +43,11 @@ struct e2d_adjoint_batch {
   std::vector<long long> grad_off;
   long long grad_elems = 0;
   double* u0 = nullptr;
+  // primitives beside the forward ping-pong states of every problem (the fast
+  // forward step, as the ensemble's), at u0_off offsets, two pools; null when
+  // they could not be allocated
+  double* qping = nullptr;
+  size_t q_total = 0;
   double* slab = nullptr;  // all problems' buffers, allocated by ensure()
   int kseg = 0, nchk = 0, cap_steps = 0;
   AdjProb* d_probs = nullptr;          // by problem index
@@ -222,6 +227,8 @@ int ensure(e2d_adjoint_batch* b, int nsteps) {
     F.nty = (b->params[p].ny + fty - 1) / fty;
     F.tile_begin = ft;
     F.id = p;
+    F.q = b->qping ? b->qping + b->u0_off[p] : nullptr;
+    F.q2 = b->qping ? b->qping + b->q_total + b->u0_off[p] : nullptr;
     ft += F.ntx * F.nty;
     const auto tape = [&](int j, bool only) {
       return b->tapes ? tape_at(b->tapes + tape_off[p], j, (long long)b->plane[p], (int)b->pitch[p], only)
@@ -301,6 +308,11 @@ void enqueue_forward(e2d_adjoint_batch* b, int nsteps, double xc, double yc, dou
     Field<double> u = field(b, p, host_buf(b, p, kPing));
     launch_dt_reduce<double>(b->hd[p], u, &b->ctls[p], 0, s);  // main.f90:42
     launch_boundaries<double>(b->hd[p], u, s);                 // main.f90:46
+    if (b->qping) {  // the primitives of both ping-pong states (the second for its corners)
+      launch_prim<double>(b->hd[p], u, field(b, p, b->qping + b->u0_off[p]), s);
+      launch_prim<double>(b->hd[p], field(b, p, host_buf(b, p, kPing + 1)),
+                          field(b, p, b->qping + b->q_total + b->u0_off[p]), s);
+    }
   }
   const int K = b->kseg, last = (nsteps + K - 1) / K - 1;
   for (int k = 0; k < nsteps; ++k) {
@@ -315,6 +327,8 @@ void enqueue_forward(e2d_adjoint_batch* b, int nsteps, double xc, double yc, dou
     L.wr = L.rd ^ 1;
     L.dt_log = b->dt_log + (size_t)k * b->nprob;
     L.inv_log = b->inv_log + (size_t)k * b->nprob;
+    // (the taping steps are the last segment's: no primitives-reading step follows them)
+    L.qin = !taping && b->qping != nullptr;
     if (taping) launch_batch_step_tape(L, s);
     else launch_batch_step<double>(0, L, s);
   }
@@ -495,6 +509,11 @@ int e2d_adjoint_batch_create(const e2d_params* base, int nprob, const int* nx, c
       cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess || batch_step_rev_setup() != 0)
     return cleanup(E2D_ERR_CUDA, "stream/event/kernel setup failed");
   cudaMemsetAsync(b->u0, 0, u0_total * sizeof(double), b->stream);
+  if (cudaMalloc(&b->qping, 2 * u0_total * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    b->qping = nullptr;
+  }
+  b->q_total = u0_total;
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return cleanup(E2D_ERR_CUDA, "initialisation failed");
   *out = b;
   return E2D_OK;
@@ -506,6 +525,7 @@ int e2d_adjoint_batch_destroy(e2d_adjoint_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   free_slab(b);
   cudaFree(b->u0);
+  cudaFree(b->qping);
   cudaFree(b->ctls);
   cudaFree(b->J);
   cudaFree(b->part_v);
