@@ -273,55 +273,61 @@ __global__ void k_trace_v1(Hydro<Real> h, Field<Real> q, StepDt<Real> sd, Ctl* c
   trace_face<Real, true>(h, qc, dqy, s, dtdy, f);  store4(qyp, j, i, f);
 }
 
-// implementationVersion 1, flux + update stage: a TX x TY tile of interior
-// cells solves the (TX+1) x TY x-faces and TX x (TY+1) y-faces it needs into
-// shared memory, then applies updateHydro.
+// implementationVersion 1, flux + update stage: a 32 x 7 tile of interior
+// cells solves the 33 x 7 x-faces and 32 x 8 y-faces it needs into shared
+// memory, then applies updateHydro.  256 threads take the faces in two
+// rounds, the y faces from a 32-face boundary (no warp issues both
+// directions' solvers, and no round is left with a few faces).
+constexpr int V1_TX = 32, V1_TY = 7, V1_NT = 256;
 template <typename Real>
-__global__ void __launch_bounds__(BX * BY) k_flux_update_v1(Hydro<Real> h, Field<Real> in, Field<Real> qxm,
-                                                            Field<Real> qxp, Field<Real> qym, Field<Real> qyp,
-                                                            Field<Real> out, StepDt<Real> sd, Ctl* ctl) {
-  constexpr int TX = BX, TY = BY;
+__global__ void __launch_bounds__(V1_NT) k_flux_update_v1(Hydro<Real> h, Field<Real> in, Field<Real> qxm,
+                                                          Field<Real> qxp, Field<Real> qym, Field<Real> qyp,
+                                                          Field<Real> out, StepDt<Real> sd, Ctl* ctl) {
+  constexpr int TX = V1_TX, TY = V1_TY, NT = V1_NT;
+  constexpr int NXF = (TX + 1) * TY, Y0 = (NXF + 31) / 32 * 32, NF = Y0 + TX * (TY + 1);
+  static_assert(NF == 2 * NT && TX * TY <= NT, "two full rounds of faces, one round of cells");
   __shared__ Real sfx[4][TY][TX + 1];
   __shared__ Real sfy[4][TY + 1][TX];
-  const int tid = threadIdx.x + threadIdx.y * BX;
+  const int tid = threadIdx.x;
   const int i0 = GW + blockIdx.x * TX, j0 = GW + blockIdx.y * TY;
   const Real dt = resolve_dt(h, sd, ctl);
   const Real dtdx = Ops<Real>::div(dt, h.dx);
   const Real dtdy = Ops<Real>::div(dt, h.dy);
-  // x-faces: face f (0..TX) of row r sits between cells i0+f-1 and i0+f
-  for (int k = tid; k < (TX + 1) * TY; k += BX * BY) {
-    const int f = k % (TX + 1), r = k / (TX + 1);
-    const int i = i0 + f, j = j0 + r;
-    if (i <= h.nx + 2 && j <= h.ny + 1) {
-      Real ql[4], qr[4], flux[4];
-      load4(qxp, j, i - 1, ql);
-      load4(qxm, j, i, qr);
-      riemann(h, ql, qr, flux);
+  for (int k = tid; k < NF; k += NT) {
+    if (k < NXF) {
+      // x-faces: face f (0..TX) of row r sits between cells i0+f-1 and i0+f
+      const int f = k % (TX + 1), r = k / (TX + 1);
+      const int i = i0 + f, j = j0 + r;
+      if (i <= h.nx + 2 && j <= h.ny + 1) {
+        Real ql[4], qr[4], flux[4];
+        load4(qxp, j, i - 1, ql);
+        load4(qxm, j, i, qr);
+        riemann(h, ql, qr, flux);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sfx[v][r][f] = flux[v] * dtdx;
-    }
-  }
-  // y-faces: face g (0..TY) of column c sits between cells j0+g-1 and j0+g
-  for (int k = tid; k < TX * (TY + 1); k += BX * BY) {
-    const int c = k % TX, g = k / TX;
-    const int i = i0 + c, j = j0 + g;
-    if (i <= h.nx + 1 && j <= h.ny + 2) {
-      Real ql[4], qr[4], flux[4];
-      load4(qyp, j - 1, i, ql);
-      load4(qym, j, i, qr);
-      Real t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
-      t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
-      riemann(h, ql, qr, flux);
-      t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
+        for (int v = 0; v < 4; ++v) sfx[v][r][f] = flux[v] * dtdx;
+      }
+    } else if (k >= Y0) {
+      // y-faces: face g (0..TY) of column c sits between cells j0+g-1 and j0+g
+      const int c = (k - Y0) % TX, g = (k - Y0) / TX;
+      const int i = i0 + c, j = j0 + g;
+      if (i <= h.nx + 1 && j <= h.ny + 2) {
+        Real ql[4], qr[4], flux[4];
+        load4(qyp, j - 1, i, ql);
+        load4(qym, j, i, qr);
+        Real t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
+        t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
+        riemann(h, ql, qr, flux);
+        t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sfy[v][g][c] = flux[v] * dtdy;
+        for (int v = 0; v < 4; ++v) sfy[v][g][c] = flux[v] * dtdy;
+      }
     }
   }
   __syncthreads();
-  const int c = threadIdx.x, r = threadIdx.y;
+  const int c = tid % TX, r = tid / TX;
   const int i = i0 + c, j = j0 + r;
   Real m = Real(0);
-  if (i <= h.nx + 1 && j <= h.ny + 1) {
+  if (r < TY && i <= h.nx + 1 && j <= h.ny + 1) {
     Real un[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -390,8 +396,8 @@ template <typename Real>
 void launch_flux_update_v1(const Hydro<Real>& h, Field<Real> in, Field<Real> qxm, Field<Real> qxp,
                            Field<Real> qym, Field<Real> qyp, Field<Real> out, StepDt<Real> sd, Ctl* ctl,
                            cudaStream_t s) {
-  dim3 b(BX, BY), g(cdiv(h.nx, BX), cdiv(h.ny, BY));
-  k_flux_update_v1<Real><<<g, b, 0, s>>>(h, in, qxm, qxp, qym, qyp, out, sd, ctl);
+  dim3 g(cdiv(h.nx, V1_TX), cdiv(h.ny, V1_TY));
+  k_flux_update_v1<Real><<<g, V1_NT, 0, s>>>(h, in, qxm, qxp, qym, qyp, out, sd, ctl);
 }
 
 #define E2D_INSTANTIATE(Real)                                                                                  \
