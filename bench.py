@@ -307,8 +307,9 @@ def measure_batched(E, a):
 def measure_adjoint(E, a):
     """dJ/d(initial density) of J = sum rho^2 w (Gaussian of width 0.1 at
     (0.6, 0.6)) on the diagonal-interface problem, FP64 HLLC: the gradient
-    (forward with sqrt(N) checkpoints, recomputation and reverse sweep, one
-    captured graph) against the forward run alone."""
+    (forward sweep keeping every state and its tape when they fit in memory,
+    else sqrt(N) checkpoints and recomputation; reverse sweep; one captured
+    graph) against the forward run alone."""
     n, ns = a.adjoint_nx, a.adjoint_steps
     p = E.make_params(nx=n, ny=n, gamma0=1.4, cfl=0.8, riemann_solver=E.RIEMANN_HLLC)
     with E.Adjoint(p) as A:
@@ -317,13 +318,16 @@ def measure_adjoint(E, a):
         for _ in range(3):
             A.gradient(ns, dt_mode=1)
             grads.append(A.last_ms()[1])
+        kseg, tape = A.layout()
         fwd = []
         for _ in range(3):
             A.objective(ns)
             fwd.append(A.last_ms()[0])
     g, f = min(grads), min(fwd)
-    return {"workload": f"{n}x{n} FP64 HLLC, {ns} steps, dt through the running CFL maximum, "
-                        f"checkpoints every {math.ceil(math.sqrt(ns))} steps",
+    layout = ("every state and its tape kept by the forward sweep, nothing recomputed" if kseg >= ns
+              else f"checkpoints every {kseg} steps, segments recomputed")
+    layout += "" if tape else ", reverse steps recomputing their forward values"
+    return {"workload": f"{n}x{n} FP64 HLLC, {ns} steps, dt through the running CFL maximum, {layout}",
             "gradient_ms": round(g, 3), "forward_ms": round(f, 3), "adjoint_over_forward": round(g / f, 3),
             "forward_mcells_per_s": round(n * n * ns / (f * 1e-3) / 1e6, 2)}
 

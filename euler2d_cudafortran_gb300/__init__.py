@@ -55,7 +55,7 @@ EXPORTED_SYMBOLS = [
     "e2d_batch_download_state", "e2d_batch_advance", "e2d_batch_last_advance_ms", "e2d_batch_set_schedule",
     "e2d_batch_get_schedule", "e2d_batch_tune", "e2d_batch_get_health",
     "e2d_adjoint_create", "e2d_adjoint_destroy", "e2d_adjoint_objective", "e2d_adjoint_gradient",
-    "e2d_adjoint_last_ms",
+    "e2d_adjoint_last_ms", "e2d_adjoint_layout",
     "e2d_adjoint_batch_create", "e2d_adjoint_batch_destroy", "e2d_adjoint_batch_init_diagonal",
     "e2d_adjoint_batch_upload_state", "e2d_adjoint_batch_objective", "e2d_adjoint_batch_gradient",
     "e2d_adjoint_batch_last_ms",
@@ -145,6 +145,7 @@ def load_library(path: str = LIB_PATH):
         "e2d_adjoint_objective": [vp, vp, i, d, d, d, dp, dp],
         "e2d_adjoint_gradient": [vp, vp, i, i, d, d, d, dp, dp, dp],
         "e2d_adjoint_last_ms": [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+        "e2d_adjoint_layout": [vp, ip, ip],
         "e2d_adjoint_batch_create": [ctypes.POINTER(Params), i, ip, ip, ip, ctypes.POINTER(vp)],
         "e2d_adjoint_batch_destroy": [vp],
         "e2d_adjoint_batch_init_diagonal": [vp, dp, dp, dp, dp, dp],
@@ -469,6 +470,13 @@ class Adjoint:
         _check(self._lib.e2d_adjoint_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def layout(self):
+        """(steps between checkpoints, tape in use) of the last gradient call;
+        the first equals the step count when every state and tape were kept."""
+        k, t = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.e2d_adjoint_layout(self._h, ctypes.byref(k), ctypes.byref(t)))
+        return k.value, bool(t.value)
+
 
 class AdjointBatch:
     """The discrete adjoint of an ensemble of FP64 HLLC problems of uneven
@@ -564,8 +572,9 @@ def selftest_wait(limit_cycles: int = 1 << 24):
 
 def selftest_arith(op: int, mode: int, n: int, seed: int = 1, rates: bool = False):
     """Bitwise check of the integer-pipe division (op 0) / square root (op 1)
-    against the hardware, or of the exponent-test pressure floor (op 2) against
-    the product and maximum, on n inputs; returns (mismatches, first_bad[4], rates)."""
+    against the hardware, or of the exponent-test pressure floor (op 2) and
+    limiter sign test (op 3) against the product (and maximum), on n inputs;
+    returns (mismatches, first_bad[4], rates)."""
     bad = ctypes.c_ulonglong()
     first = (ctypes.c_double * 4)()
     em, na = ctypes.c_double(), ctypes.c_double()

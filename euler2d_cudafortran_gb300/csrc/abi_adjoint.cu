@@ -9,7 +9,9 @@
 // from the last state of the segment back to its first, while the previous
 // segment's states are recomputed from its checkpoint with the logged dt (bit
 // for bit the forward states) on a second stream into a second set of
-// segment buffers.  The whole gradient is one captured graph.  dt_mode 0 keeps every dt
+// segment buffers.  When all N states and their tapes fit in half the free
+// device memory, the forward sweep keeps them all instead and the reverse
+// sweep recomputes nothing.  The whole gradient is one captured graph.  dt_mode 0 keeps every dt
 // frozen; dt_mode 1 also differentiates dt_n = cfl / inv_n through the
 // running maximum: the adjoint of inv_n goes to the cell whose compute_dt
 // term set that maximum, in the state where it was first reached.
@@ -106,37 +108,59 @@ void free_buffers(e2d_adjoint* a) {
 }
 
 // Buffers for nsteps: 2 ping-pong states, ceil(N/K) checkpoints, and two
-// sets of K segment states (one being reversed while the next is recomputed).
+// sets of K segment states (one being reversed while the next is recomputed)
+// with their tapes.  When every state and its tape fit in half the free
+// device memory (and E2D_ADJ_FULL_TAPE is not 0), the run is one segment
+// instead: K = N, one set, and the forward sweep keeps all N states and
+// writes all N tapes, so the reverse sweep recomputes nothing.
 int ensure(e2d_adjoint* a, int nsteps) {
   if (nsteps <= a->cap_steps) return E2D_OK;
   free_buffers(a);
-  const int K = std::max(1, (int)std::ceil(std::sqrt((double)nsteps)));
-  const int nchk = (nsteps + K - 1) / K;
-  const int nstates = 2 + nchk + 2 * K;
-  if (cudaMalloc(&a->pool, (size_t)nstates * a->state_elems * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&a->dt_log, nsteps * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&a->inv_log, nsteps * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&a->dtbar_log, nsteps * sizeof(double)) != cudaSuccess) {
-    cudaGetLastError();
-    free_buffers(a);
-    return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint checkpoints failed");
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const size_t full_bytes =
+      ((size_t)nsteps * (kTapePlanes * a->plane + a->state_elems) + (size_t)3 * a->state_elems) * sizeof(double);
+  const char* ft = std::getenv("E2D_ADJ_FULL_TAPE");
+  bool full = a->use_tape && !(ft && ft[0] == '0') && full_bytes <= free_b / 2;
+  for (;;) {
+    const int K = full ? nsteps : std::max(1, (int)std::ceil(std::sqrt((double)nsteps)));
+    const int nsets = full ? 1 : 2;
+    const int nchk = (nsteps + K - 1) / K;
+    const int nstates = 2 + nchk + nsets * K;
+    if (cudaMalloc(&a->pool, (size_t)nstates * a->state_elems * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&a->dt_log, nsteps * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&a->inv_log, nsteps * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&a->dtbar_log, nsteps * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      free_buffers(a);
+      if (full) {  // the segmented layout needs less
+        full = false;
+        continue;
+      }
+      return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint checkpoints failed");
+    }
+    const size_t tape_bytes = (size_t)nsets * K * kTapePlanes * a->plane * sizeof(double);
+    if (!a->use_tape || cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      a->tapes = nullptr;
+      if (full) {
+        free_buffers(a);
+        full = false;
+        continue;
+      }
+    } else {
+      A_CK(cudaMemsetAsync(a->tapes, 0, tape_bytes, a->stream));  // cells no tile writes read as zeros
+    }
+    A_CK(cudaMemsetAsync(a->pool, 0, (size_t)nstates * a->state_elems * sizeof(double), a->stream));
+    a->maps.resize(nstates);
+    for (int k = 0; k < nstates; ++k)
+      if (!fused_map_create<double>(a->h, state(a, k), &a->maps[k]))
+        return afail(E2D_ERR_CUDA, "TMA descriptor setup failed");
+    a->kseg = K;
+    a->nchk = nchk;
+    a->cap_steps = nsteps;
+    return E2D_OK;
   }
-  A_CK(cudaMemsetAsync(a->pool, 0, (size_t)nstates * a->state_elems * sizeof(double), a->stream));
-  const size_t tape_bytes = (size_t)2 * K * kTapePlanes * a->plane * sizeof(double);
-  if (!a->use_tape || cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
-    cudaGetLastError();
-    a->tapes = nullptr;
-  } else {
-    A_CK(cudaMemsetAsync(a->tapes, 0, tape_bytes, a->stream));  // cells no tile writes read as zeros
-  }
-  a->maps.resize(nstates);
-  for (int k = 0; k < nstates; ++k)
-    if (!fused_map_create<double>(a->h, state(a, k), &a->maps[k]))
-      return afail(E2D_ERR_CUDA, "TMA descriptor setup failed");
-  a->kseg = K;
-  a->nchk = nchk;
-  a->cap_steps = nsteps;
-  return E2D_OK;
 }
 
 constexpr int kPing = 0;  // states 0, 1: forward ping-pong
@@ -473,6 +497,13 @@ int e2d_adjoint_last_ms(e2d_adjoint* a, float* objective_ms, float* gradient_ms)
   if (!a) return afail(E2D_ERR_INVALID_ARG, "null adjoint handle");
   if (objective_ms) *objective_ms = a->last_forward_ms;
   if (gradient_ms) *gradient_ms = a->last_gradient_ms;
+  return E2D_OK;
+}
+
+int e2d_adjoint_layout(e2d_adjoint* a, int* segment_steps, int* tape) {
+  if (!a) return afail(E2D_ERR_INVALID_ARG, "null adjoint handle");
+  if (segment_steps) *segment_steps = a->kseg;
+  if (tape) *tape = a->tapes ? 1 : 0;
   return E2D_OK;
 }
 

@@ -424,37 +424,47 @@ __device__ __forceinline__ void argmax_part(const Hydro<double>& h, Field<double
       const long long idx = (long long)j * h.isize + i;
       if (t > best || (t == best && idx < bi)) { best = t; bi = idx; }
     }
-  __shared__ double sv[256];
-  __shared__ long long si[256];
-  sv[threadIdx.x] = best;
-  si[threadIdx.x] = bi;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      const double v2 = sv[threadIdx.x + s];
-      const long long i2 = si[threadIdx.x + s];
-      if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
-        sv[threadIdx.x] = v2;
-        si[threadIdx.x] = i2;
-      }
-    }
-    __syncthreads();
+  // (largest term, lowest index) is a total order: any reduction order gives
+  // the same cell
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(0xffffffffu, best, o);
+    const long long i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (v2 > best || (v2 == best && i2 < bi)) { best = v2; bi = i2; }
   }
-  if (threadIdx.x == 0) { pv[part] = sv[0]; pi[part] = si[0]; }
+  __shared__ double sv[32];
+  __shared__ long long si[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { sv[warp] = best; si[warp] = bi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; ++w)
+      if (sv[w] > best || (sv[w] == best && si[w] < bi)) { best = sv[w]; bi = si[w]; }
+    pv[part] = best;
+    pi[part] = bi;
+  }
 }
 
 // If the running maximum rises at state m, the steps [m, n1) up to the next
 // rise use the compute_dt term of the argmax cell of state m; their dt
 // adjoints go to Ubar_m: dt_n = cfl / inv_n, d dt_n / d inv_n = -cfl / inv_n^2.
-// One warp (called by all 32 lanes); logs have stride `stride`.
+// One block of kDtThreads threads (all call it); logs have stride `stride`.
+// The partial maxima, the search for n1 and the sum are spread over the
+// block: the routing sits between two reverse steps, so its latency is the
+// gradient's.
+constexpr int kDtThreads = 256;
 __device__ __forceinline__ void dt_route(const Hydro<double>& h, Field<double> u, Field<double> ub, const double* pv,
                                          const long long* pi, int nparts, const double* dtbar_log,
                                          const double* inv_log, int stride, int m, int nsteps) {
-  const int lane = threadIdx.x & 31;
+  constexpr int NW = kDtThreads / 32;
+  __shared__ double sbest[NW], ssum[NW];
+  __shared__ long long sidx[NW];
+  __shared__ int sn1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // the argmax over the partial results (largest term, lowest index on ties)
   double best = -1.0;
   long long bi = 0x7fffffffffffffffll;
-  for (int k = lane; k < nparts; k += 32)
+  for (int k = tid; k < nparts; k += kDtThreads)
     if (pv[k] > best || (pv[k] == best && pi[k] < bi)) { best = pv[k]; bi = pi[k]; }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -462,21 +472,35 @@ __device__ __forceinline__ void dt_route(const Hydro<double>& h, Field<double> u
     const long long i2 = __shfl_xor_sync(0xffffffffu, bi, o);
     if (v2 > best || (v2 == best && i2 < bi)) { best = v2; bi = i2; }
   }
-  // n1: the next state after m where the maximum rises (or nsteps)
-  int n1 = nsteps;
-  for (int base = m + 1; base < nsteps; base += 32) {
-    const int n = base + lane;
-    const unsigned rise = __ballot_sync(0xffffffffu, n < nsteps && max_rises(inv_log, n, stride));
-    if (rise) { n1 = base + __ffs(rise) - 1; break; }
-  }
+  if (lane == 0) { sbest[warp] = best; sidx[warp] = bi; }
+  if (tid == 0) sn1 = nsteps;
+  __syncthreads();
+  // n1: the next state after m where the maximum rises (or nsteps); a
+  // thread's first rise is the smallest of its stride
+  for (int n = m + 1 + tid; n < nsteps; n += kDtThreads)
+    if (max_rises(inv_log, n, stride)) {
+      atomicMin(&sn1, n);
+      break;
+    }
+  __syncthreads();
+  const int n1 = sn1;
   double sacc = 0.0;
-  for (int n = m + lane; n < n1; n += 32) {
+  for (int n = m + tid; n < n1; n += kDtThreads) {
     const double inv = inv_log[(long long)n * stride];
     sacc += -h.cfl / (inv * inv) * dtbar_log[(long long)n * stride];
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
-  if (lane != 0) return;
+  if (lane == 0) ssum[warp] = sacc;
+  __syncthreads();
+  if (tid != 0) return;
+  best = sbest[0];
+  bi = sidx[0];
+  sacc = ssum[0];
+  for (int w = 1; w < NW; ++w) {
+    if (sbest[w] > best || (sbest[w] == best && sidx[w] < bi)) { best = sbest[w]; bi = sidx[w]; }
+    sacc += ssum[w];
+  }
   const int j = (int)(bi / h.isize), i = (int)(bi - (long long)j * h.isize);
   double uc[4], g[4] = {0, 0, 0, 0};
 #pragma unroll
@@ -495,7 +519,7 @@ __global__ void k_argmax_partial(Hydro<double> h, Field<double> u, double* pv, l
 __global__ void k_dt_route(Hydro<double> h, Field<double> u, Field<double> ub, const double* pv,
                            const long long* pi, int nparts, const double* dtbar_log, const double* inv_log, int m,
                            int nsteps) {
-  if (!max_rises(inv_log, m, 1)) return;  // uniform over the warp
+  if (!max_rises(inv_log, m, 1)) return;  // uniform over the block
   dt_route(h, u, ub, pv, pi, nparts, dtbar_log, inv_log, 1, m, nsteps);
 }
 
@@ -586,7 +610,7 @@ __global__ void k_batch_dt_route(const AdjProb* __restrict__ probs, int nprob, c
                                  int nparts, const double* dtbar_log, const double* inv_log, int un, int ub_out,
                                  int m, int nsteps) {
   const int p = blockIdx.x;
-  if (!max_rises(inv_log + p, m, nprob)) return;  // uniform over the warp
+  if (!max_rises(inv_log + p, m, nprob)) return;  // uniform over the block
   const AdjProb& P = probs[p];
   dt_route(P.h, afield(P, un), afield(P, ub_out), pv + (long long)p * nparts, pi + (long long)p * nparts, nparts,
            dtbar_log + p, inv_log + p, nprob, m, nsteps);
@@ -670,7 +694,7 @@ void launch_argmax(const Hydro<double>& h, Field<double> u, double* pv, long lon
 void launch_dt_route(const Hydro<double>& h, Field<double> u, Field<double> ub, const double* pv, const long long* pi,
                      int nparts, const double* dtbar_log, const double* inv_log, int m, int nsteps,
                      cudaStream_t s) {
-  k_dt_route<<<1, 32, 0, s>>>(h, u, ub, pv, pi, nparts, dtbar_log, inv_log, m, nsteps);
+  k_dt_route<<<1, kDtThreads, 0, s>>>(h, u, ub, pv, pi, nparts, dtbar_log, inv_log, m, nsteps);
 }
 
 void launch_objective(const Hydro<double>& h, Field<double> u, double xc, double yc, double sig, double* J,
@@ -712,7 +736,7 @@ void launch_batch_argmax(const AdjBatch& B, int un, int m, cudaStream_t s) {
 }
 
 void launch_batch_dt_route(const AdjBatch& B, int un, int ub_out, int m, int nsteps, cudaStream_t s) {
-  k_batch_dt_route<<<B.nprob, 32, 0, s>>>(B.probs, B.nprob, B.part_v, B.part_i, B.nparts, B.dtbar_log, B.inv_log, un,
+  k_batch_dt_route<<<B.nprob, kDtThreads, 0, s>>>(B.probs, B.nprob, B.part_v, B.part_i, B.nparts, B.dtbar_log, B.inv_log, un,
                                           ub_out, m, nsteps);
 }
 

@@ -36,7 +36,10 @@ __device__ bool same(double x, double y) {
 }
 
 // op 0: division, op 1: square root, op 2: the pressure floor max(a, b*c)
-// (against the emulated maximum of the hardware product).  Modes 0-2 as
+// (against the emulated maximum of the hardware product), op 3: the
+// limiter's sign test dlft*drgt <= 0 from signs and exponents (the product
+// taken where it reports the undecided band), against the product (mode 3:
+// exponent sums next to the underflow band, either sign).  Modes 0-2 as
 // rand_double; mode 4 signed zeros and small integers; mode 3 builds
 // operands whose exact result lies within one part in 2^60 of a rounding
 // boundary (quotient q + 1/2 ulp times b, or (q + 1/2 ulp)^2), and for op 2
@@ -62,6 +65,26 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       const double x = e2d::floor_prod<double>(a, b, c);
       const double y = e2d::emul::max_i(a, __dmul_rn(b, c));
       if (!same(x, y)) {
+        if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
+      }
+      continue;
+    }
+    if (op == 3) {
+      a = rand_double(r1, mode == 3 ? 0 : mode == 4 ? 2 : mode);
+      b = rand_double(r2, mode == 3 ? 0 : mode == 4 ? 0 : mode);
+      if (mode == 3) {  // biased exponent sum within 966..975, subnormal and zero factors among them
+        const long long ea = (long long)(r1 % 976);
+        const long long eb = 966 + (long long)(r2 % 10) - ea;
+        a = __longlong_as_double((long long)(r1 & 0x800fffffffffffffull) | (ea << 52));
+        b = __longlong_as_double((long long)(r2 & 0x800fffffffffffffull) | ((eb < 0 ? 0 : eb > 2046 ? 2046 : eb) << 52));
+      } else if (mode == 4) {
+        a = (r1 & 2) ? ((r1 & 1) ? -0.0 : 0.0) : a;
+      }
+      bool amb = false;
+      bool x = e2d::prod_le0(a, b, amb);
+      if (amb) x = __dmul_rn(a, b) <= 0.0;
+      const bool y = __dmul_rn(a, b) <= 0.0;
+      if (x != y) {
         if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
       }
       continue;
@@ -162,7 +185,7 @@ extern "C" int e2d_selftest_wait(long long limit_cycles, int* arrived_completed,
 extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* first_bad, double* emulated_per_s,
                                   double* native_per_s) {
-  if (op < 0 || op > 2 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
+  if (op < 0 || op > 3 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {

@@ -214,38 +214,76 @@ __device__ __forceinline__ Real cell_invdt(const Hydro<Real>& h, const Real u[4]
 // dcen >= 0, dlim = 0 if dlft*drgt <= 0 else min(|dlft|,|drgt|), and the
 // slope dsgn*min(dlim,|dcen|).  st is 1 or 2; the products by st, 0.5 and
 // dsgn are exact scalings and sign flips.
-// dlim = (dlft*drgt <= 0) ? 0 : slop, slop = min(|dlft|, |drgt|).  (Deciding
-// the product's sign from signs and exponents on the integer pipe was
-// measured slower: the compiler predicates the rare IEEE fallback, and a
-// predicated FP64 instruction still takes its FP64 pipe slots.)
 template <typename Real>
 __device__ __forceinline__ Real limiter_dlim(Real dlft, Real drgt, Real slop) {
   return Ops<Real>::le0(dlft * drgt) ? Real(0.0) : slop;
 }
 
-template <typename Real>
-__device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm) {
+// dlft*drgt <= 0 for double, decided without the product: true when either
+// factor is a zero or the signs differ; for same-sign nonzero normal factors
+// with biased exponents ea, eb the exact product lies in
+// [2^(ea+eb-2046), 2^(ea+eb-2044)), so it rounds to +0 when ea+eb <= 969 and
+// to a nonzero value when ea+eb >= 972.  Exponent sums in between,
+// subnormal factors, and infinite or NaN factors (0 * inf is NaN, and
+// NaN <= 0 is false) set `amb`: the caller then takes the product.
+#ifndef E2D_LIM_INT
+#define E2D_LIM_INT 1
+#endif
+__device__ __forceinline__ bool prod_le0(double a, double b, bool& amb) {
+#ifdef E2D_FP64_NATIVE
+  return a * b <= 0.0;
+#else
+  const uint64_t ia = emul::bits(a), ib = emul::bits(b);
+  const int ea = (int)(ia >> 52) & 0x7ff, eb = (int)(ib >> 52) & 0x7ff;
+  const bool zero = ((ia << 1) == 0) | ((ib << 1) == 0);
+  const bool neg = (int64_t)(ia ^ ib) < 0;
+  const int e = ea + eb;
+  amb |= (ea == 0x7ff) | (eb == 0x7ff) | (!zero & ((ea == 0) | (eb == 0) | ((unsigned)(e - 970) < 2u)));
+  return zero | neg | (e <= 969);
+#endif
+}
+
+template <typename Real, bool INT = false>
+__device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm, bool& amb) {
   using O = Ops<Real>;
   const Real dl = q - qm, dr = qp - q;
   const Real dlft = mc ? O::twice(dl) : dl;
   const Real drgt = mc ? O::twice(dr) : dr;
   const Real dcen = O::half(qp - qm);
   const Real slop = O::min(rabs(dlft), rabs(drgt));
-  const Real dlim = limiter_dlim(dlft, drgt, slop);
+  Real dlim;
+  if constexpr (INT) dlim = prod_le0(dlft, drgt, amb) ? Real(0.0) : slop;
+  else dlim = limiter_dlim(dlft, drgt, slop);
   return O::neg_if(O::min(dlim, rabs(dcen)), !O::ge0(dcen));
 }
 
-// slope_unsplit_hydro_2d, serial_ref/m_utils.f90:268-342.
+// slope_unsplit_hydro_2d, serial_ref/m_utils.f90:268-342.  For double the
+// limiter's sign test is decided from signs and exponents (prod_le0); a
+// cell with a factor pair in the undecided band recomputes its slopes with
+// the products, in a branch of its own -- a fallback product beside each
+// test would be predicated into every path, and a predicated FP64
+// instruction still takes its FP64 pipe slot.
 template <typename Real>
 __device__ __forceinline__ void slopes(const Hydro<Real>& h, const Real q[4], const Real qpx[4],
                                        const Real qmx[4], const Real qpy[4], const Real qmy[4],
                                        Real dqx[4], Real dqy[4]) {
   if (h.slope_type == 1 || h.slope_type == 2) {
     const bool mc = h.slope_type == 2;
+    bool amb = false;
+    constexpr bool INT = sizeof(Real) == 8 && E2D_LIM_INT;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      dqx[v] = slope1(mc, q[v], qpx[v], qmx[v]);
-      dqy[v] = slope1(mc, q[v], qpy[v], qmy[v]);
+      dqx[v] = slope1<Real, INT>(mc, q[v], qpx[v], qmx[v], amb);
+      dqy[v] = slope1<Real, INT>(mc, q[v], qpy[v], qmy[v], amb);
+    }
+    if constexpr (INT) {
+      if (amb) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          dqx[v] = slope1<Real, false>(mc, q[v], qpx[v], qmx[v], amb);
+          dqy[v] = slope1<Real, false>(mc, q[v], qpy[v], qmy[v], amb);
+        }
+      }
     }
   } else {
 #pragma unroll

@@ -136,10 +136,12 @@ int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
 
 /* Self-test of the library's integer-pipe double division (op 0) and square
  * root (op 1) against the hardware operations, and of its exponent-test
- * pressure floor max(a, b*c) (op 2) against the product and maximum, on n
- * seeded inputs (mode 0 any bit pattern, 1 exponents near 1, 2 exponents
- * within +-400, 3 results next to rounding boundaries -- for op 2, a within
- * two binades of b*c --, 4 signed zeros and small integers): *mismatches
+ * pressure floor max(a, b*c) (op 2) and limiter sign test a*b <= 0 (op 3)
+ * against the product (and maximum), on n seeded inputs (mode 0 any bit
+ * pattern, 1 exponents near 1, 2 exponents within +-400, 3 results next to
+ * rounding boundaries -- for op 2, a within two binades of b*c; for op 3,
+ * products next to the underflow to zero --, 4 signed zeros and small
+ * integers): *mismatches
  * counts results that differ in any bit, first_bad[4] (optional) = a, b,
  * library, reference operation of the first one; the two rates (optional,
  * ops 0 and 1) are chained operations per second.  Not part of the
@@ -239,6 +241,11 @@ int e2d_adjoint_gradient(e2d_adjoint* a, const void* u0, int nsteps, int dt_mode
                          double sigma, double* J, double* grad_rho0, double* dt_log);
 /* Device times (ms) of the last objective and gradient calls. */
 int e2d_adjoint_last_ms(e2d_adjoint* a, float* objective_ms, float* gradient_ms);
+/* Memory layout of the last gradient call: *segment_steps = K, the steps
+ * between checkpoints (K = N when every state and its tape were kept and
+ * nothing was recomputed); *tape = 1 when the reverse steps read the forward
+ * values from a tape, 0 when they recompute them.  Not in the reference. */
+int e2d_adjoint_layout(e2d_adjoint* a, int* segment_steps, int* tape);
 
 /* ---- Batched adjoint: the adjoint of many independent problems at once ----
  * No counterpart in the reference.  Problems of uneven sizes (FP64, HLLC),

@@ -136,3 +136,28 @@ def test_tape_gives_the_recomputed_gradient(e2d, oracle, monkeypatch, dt_mode):
     assert abs(J1 - J2) <= 1e-13 * abs(J2)  # J is summed with atomic additions
     assert np.any(g1 != 0.0)
     assert float(np.sum(np.abs(g1 - g2)) / np.sum(np.abs(g2))) <= 1e-12
+
+
+@pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
+def test_whole_tape_gives_the_segmented_gradient(e2d, oracle, monkeypatch, dt_mode):
+    """When every state and its tape fit in memory the forward sweep keeps
+    them all and nothing is recomputed; with E2D_ADJ_FULL_TAPE=0 the run is
+    checkpointed in segments whose states and tapes are recomputed during the
+    reverse sweep.  The recomputed values are bit for bit the forward's, so
+    only the order of atomic additions can differ."""
+    p = e2d.make_params(nx=72, ny=88, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
+                        boundary_type_xmin=2, boundary_type_ymax=3, boundary_type_ymin=3)
+    po = oracle.Params(nx=72, ny=88, gamma0=1.4, cfl=0.8, riemann=2, bc_xmin=2, bc_ymin=3, bc_ymax=3)
+    u0 = smooth_base(oracle, po)
+    n = 29  # K = 6 when segmented: a ragged last segment
+    with e2d.Adjoint(p) as a:
+        J1, g1, d1 = a.gradient(n, u0, dt_mode=dt_mode)
+        assert a.layout() == (n, True)
+    monkeypatch.setenv("E2D_ADJ_FULL_TAPE", "0")
+    with e2d.Adjoint(p) as b:
+        J2, g2, d2 = b.gradient(n, u0, dt_mode=dt_mode)
+        assert b.layout() == (6, True)
+    assert np.array_equal(d1, d2)
+    assert abs(J1 - J2) <= 1e-13 * abs(J2)
+    assert np.any(g1 != 0.0)
+    assert float(np.sum(np.abs(g1 - g2)) / np.sum(np.abs(g2))) <= 1e-12

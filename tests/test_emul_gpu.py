@@ -1,13 +1,14 @@
 """The integer-pipe double division and square root used by the FP64 step
 must agree bit for bit with the hardware IEEE operations, and the
-exponent-test pressure floor with the product and maximum it skips."""
+exponent-test pressure floor and limiter sign test with the products they
+skip."""
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4], ids=["any-bits", "near-1", "wide", "near-boundary", "zeros"])
-@pytest.mark.parametrize("op", [0, 1, 2], ids=["div", "sqrt", "pressure-floor"])
+@pytest.mark.parametrize("op", [0, 1, 2, 3], ids=["div", "sqrt", "pressure-floor", "limiter-sign"])
 def test_emulated_matches_hardware(e2d, op, mode):
     bad, first, _ = e2d.selftest_arith(op, mode, 1 << 26, seed=12345 + 17 * mode + op)
     assert bad == 0, f"{bad} mismatches; first (a, b, emulated, hardware) = {first}"
