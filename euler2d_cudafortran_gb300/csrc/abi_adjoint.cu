@@ -50,6 +50,7 @@ struct e2d_adjoint {
   StateMap qmaps[2];
   std::map<std::tuple<int, double, double, double>, cudaGraphExec_t> fwd_graphs;
   int nchk = 0, kseg = 0, cap_steps = 0;
+  bool cap_gradient = false;  // the buffers were laid out for a gradient (tapes considered)
   std::vector<StateMap> maps;  // one TMA descriptor per state buffer
   double* ub[3] = {nullptr, nullptr, nullptr};  // adjoint states, rotating: read, written, zeroed
   Ctl* ctl = nullptr;
@@ -105,6 +106,7 @@ void free_buffers(e2d_adjoint* a) {
   a->dt_log = a->inv_log = a->dtbar_log = nullptr;
   a->maps.clear();
   a->cap_steps = 0;
+  a->cap_gradient = false;
 }
 
 // Buffers for nsteps: 2 ping-pong states, ceil(N/K) checkpoints, and two
@@ -112,16 +114,18 @@ void free_buffers(e2d_adjoint* a) {
 // with their tapes.  When every state and its tape fit in half the free
 // device memory (and E2D_ADJ_FULL_TAPE is not 0), the run is one segment
 // instead: K = N, one set, and the forward sweep keeps all N states and
-// writes all N tapes, so the reverse sweep recomputes nothing.
-int ensure(e2d_adjoint* a, int nsteps) {
-  if (nsteps <= a->cap_steps) return E2D_OK;
+// writes all N tapes, so the reverse sweep recomputes nothing.  A call for
+// the objective alone (gradient false) lays out no tape; a later gradient
+// lays the buffers out again.
+int ensure(e2d_adjoint* a, int nsteps, bool gradient) {
+  if (nsteps <= a->cap_steps && (a->cap_gradient || !gradient)) return E2D_OK;
   free_buffers(a);
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   const size_t full_bytes =
       ((size_t)nsteps * (kTapePlanes * a->plane + a->state_elems) + (size_t)3 * a->state_elems) * sizeof(double);
   const char* ft = std::getenv("E2D_ADJ_FULL_TAPE");
-  bool full = a->use_tape && !(ft && ft[0] == '0') && full_bytes <= free_b / 2;
+  bool full = gradient && a->use_tape && !(ft && ft[0] == '0') && full_bytes <= free_b / 2;
   for (;;) {
     const int K = full ? nsteps : std::max(1, (int)std::ceil(std::sqrt((double)nsteps)));
     const int nsets = full ? 1 : 2;
@@ -140,7 +144,7 @@ int ensure(e2d_adjoint* a, int nsteps) {
       return afail(E2D_ERR_OOM, "cudaMalloc of the adjoint checkpoints failed");
     }
     const size_t tape_bytes = (size_t)nsets * K * kTapePlanes * a->plane * sizeof(double);
-    if (!a->use_tape || cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
+    if (!gradient || !a->use_tape || cudaMalloc(&a->tapes, tape_bytes) != cudaSuccess) {
       cudaGetLastError();
       a->tapes = nullptr;
       if (full) {
@@ -159,6 +163,7 @@ int ensure(e2d_adjoint* a, int nsteps) {
     a->kseg = K;
     a->nchk = nchk;
     a->cap_steps = nsteps;
+    a->cap_gradient = gradient;
     return E2D_OK;
   }
 }
@@ -405,7 +410,7 @@ int e2d_adjoint_objective(e2d_adjoint* a, const void* u0, int nsteps, double xc,
                           const double* dt_fixed, double* J) {
   if (!a || !J || nsteps < 1 || !(sigma > 0.0)) return afail(E2D_ERR_INVALID_ARG, "bad objective arguments");
   cudaSetDevice(a->device);
-  if (int rc = ensure(a, nsteps)) return rc;
+  if (int rc = ensure(a, nsteps, false)) return rc;
   if (int rc = load_initial(a, u0)) return rc;
   // replayed from a captured graph on later calls with the same step count and
   // objective (not with given dt values)
@@ -447,7 +452,7 @@ int e2d_adjoint_gradient(e2d_adjoint* a, const void* u0, int nsteps, int dt_mode
   if (!a || !J || !grad_rho0 || nsteps < 1 || (dt_mode != 0 && dt_mode != 1) || !(sigma > 0.0))
     return afail(E2D_ERR_INVALID_ARG, "bad gradient arguments");
   cudaSetDevice(a->device);
-  if (int rc = ensure(a, nsteps)) return rc;
+  if (int rc = ensure(a, nsteps, true)) return rc;
   if (int rc = load_initial(a, u0)) return rc;
   cudaStream_t s = a->stream;
   // The forward/backward pair is one captured graph, replayed on later calls

@@ -161,3 +161,23 @@ def test_whole_tape_gives_the_segmented_gradient(e2d, oracle, monkeypatch, dt_mo
     assert abs(J1 - J2) <= 1e-13 * abs(J2)
     assert np.any(g1 != 0.0)
     assert float(np.sum(np.abs(g1 - g2)) / np.sum(np.abs(g2))) <= 1e-12
+
+
+def test_objective_before_gradient(e2d, oracle):
+    """A forward-only call lays out no tape; a gradient on the same handle
+    afterwards lays the buffers out for itself and matches a fresh handle's."""
+    p = e2d.make_params(nx=64, ny=48, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC)
+    po = oracle.Params(nx=64, ny=48, gamma0=1.4, cfl=0.8, riemann=2)
+    u0 = smooth_base(oracle, po)
+    n = 12
+    with e2d.Adjoint(p) as a:
+        Jo = a.objective(n, u0)
+        assert a.layout()[1] is False
+        J1, g1, d1 = a.gradient(n, u0, dt_mode=1)
+        assert a.layout() == (n, True)
+        assert abs(a.objective(n, u0) - Jo) <= 1e-13 * abs(Jo)  # J is summed with atomic additions
+    with e2d.Adjoint(p) as b:
+        J2, g2, d2 = b.gradient(n, u0, dt_mode=1)
+    assert abs(Jo - J2) <= 1e-13 * abs(J2) and abs(J1 - J2) <= 1e-13 * abs(J2)
+    assert np.array_equal(d1, d2)
+    assert float(np.sum(np.abs(g1 - g2)) / np.sum(np.abs(g2))) <= 1e-12
