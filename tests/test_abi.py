@@ -114,6 +114,8 @@ def test_adjoint_create_rejects_invalid_arguments(e2d):
     assert lib.e2d_adjoint_batch_destroy(None) == e2d.E2D_OK
     J = ctypes.c_double()
     assert lib.e2d_adjoint_batch_objective(None, 10, 0.6, 0.6, 0.1, ctypes.byref(J)) == e2d.E2D_ERR_INVALID_ARG
+    k, t = ctypes.c_int(), ctypes.c_int()
+    assert lib.e2d_adjoint_layout(None, ctypes.byref(k), ctypes.byref(t)) == e2d.E2D_ERR_INVALID_ARG
 
 
 def test_async_download_and_selftest_reject_invalid_arguments(e2d):
