@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--precision", type=int, choices=[4, 8], default=8)
     ap.add_argument("--version", type=int, choices=[0, 1, 2], default=0)
     ap.add_argument("--riemann", choices=["hllc", "approx"], default="hllc")
+    ap.add_argument("--arith", choices=["exact", "fma"], default="exact",
+                    help="library build: exact (bitwise serial_ref arithmetic) or fma (multiply-adds fused)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
@@ -172,11 +174,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_value(precision: int, nx: int, version: int, key: str):
+def profiled_value(precision: int, nx: int, version: int, key: str, arith: str = "exact"):
     """A per-launch figure of the step kernel (`dram_bytes_per_launch`,
-    `fp64_warp_inst_per_launch`) from the committed ncu summary of the same
-    workload, if there is one."""
-    name = f"k_fused_{nx}_{'fp64' if precision == 8 else 'fp32'}_traffic.txt" if version == 0 else None
+    `fp64_warp_inst_per_launch`, `thread_inst_per_cell`) from the committed
+    ncu summary of the same workload and library build, if there is one."""
+    suffix = "_fma" if arith == "fma" else ""
+    name = f"k_fused_{nx}_{'fp64' if precision == 8 else 'fp32'}{suffix}_traffic.txt" if version == 0 else None
     if not name:
         return None
     path = os.path.join(ROOT, "profiles", name)
@@ -188,8 +191,8 @@ def profiled_value(precision: int, nx: int, version: int, key: str):
     return None
 
 
-def profiled_traffic(precision: int, nx: int, version: int):
-    return profiled_value(precision, nx, version, "dram_bytes_per_launch")
+def profiled_traffic(precision: int, nx: int, version: int, arith: str = "exact"):
+    return profiled_value(precision, nx, version, "dram_bytes_per_launch", arith)
 
 
 def workload_name(a):
@@ -217,6 +220,15 @@ def time_oracle(a, nsteps: int, nthreads: int):
 
 # ---------------------------------------------------------------- reference arm
 
+def bench_config(a, ws: int):
+    """The workload description both arms print (identical dicts)."""
+    isz = a.nx + 4
+    return {"workload": workload_name(a), "nx": a.nx, "ny": a.nx, "steps": a.steps,
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "l2": "inputs larger than L2 (u and u2: 2 x %.1f MB ping-pong per step)"
+                  % (4 * isz * isz * a.precision / 1e6)}
+
+
 def run_reference(a, dist):
     if dist.rank != 0:
         return
@@ -225,7 +237,7 @@ def run_reference(a, dist):
     nthreads = os.cpu_count() or 1
     cells = a.nx * a.nx
     if a.warmup:
-        time_oracle(a, max(1, min(a.warmup, 2)), nthreads)
+        time_oracle(a, a.warmup, nthreads)
     t = time_oracle(a, a.steps, nthreads)
     v = cells * a.steps / t / 1e6
     line = {
@@ -233,10 +245,11 @@ def run_reference(a, dist):
         "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1e3 * t / a.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if a.precision == 8 else "f32", "data": "synthetic",
-        "config": {"workload": workload_name(a), "nx": a.nx, "ny": a.nx},
+        "config": bench_config(a, dist.ws),
         "cpu_baseline": {"value": round(v, 3), "unit": "Mcell-updates/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{a.nx}x{a.nx}, {a.steps} steps: CPU restatement of serial_ref (no Fortran "
-                                   f"compiler on the box) with OpenMP on the do-concurrent loops of stdpar"},
+                         "sample": f"{a.nx}x{a.nx}, {a.steps} steps after {a.warmup} warm-up steps: CPU "
+                                   f"restatement of serial_ref (no Fortran compiler on the box) with OpenMP on "
+                                   f"the do-concurrent loops of stdpar"},
         "e2e": {"value": round(v, 3), "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -255,7 +268,8 @@ def measure_batched(E, a):
     n = a.batched_steps
     riemann = E.RIEMANN_HLLC if a.riemann == "hllc" else E.RIEMANN_APPROX
     init = (ens.offset, ens.rho_hi, ens.p_hi, ens.rho_lo, ens.p_lo)
-    with E.Batch(ens.sizes, ens.bcs, gamma0=1.4, cfl=0.8, riemann_solver=riemann, precision=a.precision) as b:
+    with E.Batch(ens.sizes, ens.bcs, gamma0=1.4, cfl=0.8, riemann_solver=riemann, precision=a.precision,
+                 arith=a.arith) as b:
         b.init_diagonal(*init)
         t0 = time.perf_counter()
         b.tune(steps=3)
@@ -273,7 +287,7 @@ def measure_batched(E, a):
         p = E.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=riemann, precision=a.precision,
                           boundary_type_xmin=bc[0], boundary_type_xmax=bc[1], boundary_type_ymin=bc[2],
                           boundary_type_ymax=bc[3])
-        with E.HydroRun(p) as run:
+        with E.HydroRun(p, arith=a.arith) as run:
             run.init_diagonal(*(x[k] for x in init))
             run.advance(0, n, log=False)
             plain_ms += run.last_advance_ms()
@@ -304,31 +318,42 @@ def measure_batched(E, a):
 
 # ---------------------------------------------------------------- adjoints
 
-def measure_adjoint(E, a):
+def measure_adjoint(E, a, full_tape: bool = True):
     """dJ/d(initial density) of J = sum rho^2 w (Gaussian of width 0.1 at
     (0.6, 0.6)) on the diagonal-interface problem, FP64 HLLC: the gradient
-    (forward sweep keeping every state and its tape when they fit in memory,
-    else sqrt(N) checkpoints and recomputation; reverse sweep; one captured
-    graph) against the forward run alone."""
+    (one captured graph: forward sweep, reverse sweep) against the forward
+    run alone.  full_tape: the forward sweep keeps every state and its tape
+    when they fit in memory; otherwise (and with full_tape False, the
+    sqrt(N)-checkpoint method) a state copy every ceil(sqrt(N)) steps and the
+    segments recomputed during the reverse sweep."""
     n, ns = a.adjoint_nx, a.adjoint_steps
     p = E.make_params(nx=n, ny=n, gamma0=1.4, cfl=0.8, riemann_solver=E.RIEMANN_HLLC)
-    with E.Adjoint(p) as A:
-        A.gradient(ns, dt_mode=1)  # captures the graph
-        grads = []
-        for _ in range(3):
-            A.gradient(ns, dt_mode=1)
-            grads.append(A.last_ms()[1])
-        kseg, tape = A.layout()
-        fwd = []
-        for _ in range(3):
-            A.objective(ns)
-            fwd.append(A.last_ms()[0])
+    old = os.environ.get("E2D_ADJ_FULL_TAPE")
+    os.environ["E2D_ADJ_FULL_TAPE"] = "1" if full_tape else "0"
+    try:
+        with E.Adjoint(p, arith=a.arith) as A:
+            A.gradient(ns, dt_mode=1)  # captures the graph
+            grads = []
+            for _ in range(3):
+                A.gradient(ns, dt_mode=1)
+                grads.append(A.last_ms()[1])
+            kseg, tape = A.layout()
+            fwd = []
+            for _ in range(3):
+                A.objective(ns)
+                fwd.append(A.last_ms()[0])
+    finally:
+        if old is None:
+            os.environ.pop("E2D_ADJ_FULL_TAPE", None)
+        else:
+            os.environ["E2D_ADJ_FULL_TAPE"] = old
     g, f = min(grads), min(fwd)
     layout = ("every state and its tape kept by the forward sweep, nothing recomputed" if kseg >= ns
-              else f"checkpoints every {kseg} steps, segments recomputed")
+              else f"sqrt(N) checkpoints (every {kseg} steps), segments recomputed during the reverse sweep")
     layout += "" if tape else ", reverse steps recomputing their forward values"
     return {"workload": f"{n}x{n} FP64 HLLC, {ns} steps, dt through the running CFL maximum, {layout}",
-            "gradient_ms": round(g, 3), "forward_ms": round(f, 3), "adjoint_over_forward": round(g / f, 3),
+            "segment_steps": kseg, "gradient_ms": round(g, 3), "forward_ms": round(f, 3),
+            "adjoint_over_forward": round(g / f, 3),
             "forward_mcells_per_s": round(n * n * ns / (f * 1e-3) / 1e6, 2)}
 
 
@@ -340,7 +365,7 @@ def measure_adjoint_batch(E, a):
     ens = diagonal_ensemble(32, 2024, sides=tuple(range(256, 1025, 64)))
     ns = a.adjoint_batch_steps
     init = (ens.offset, ens.rho_hi, ens.p_hi, ens.rho_lo, ens.p_lo)
-    with E.AdjointBatch(ens.sizes, ens.bcs, gamma0=1.4, cfl=0.8) as B:
+    with E.AdjointBatch(ens.sizes, ens.bcs, gamma0=1.4, cfl=0.8, arith=a.arith) as B:
         B.init_diagonal(*init)
         B.gradient(ns, dt_mode=1)  # captures the graph
         B.gradient(ns, dt_mode=1)
@@ -358,15 +383,42 @@ def measure_adjoint_batch(E, a):
 
 # ---------------------------------------------------------------- our arm
 
+def time_run(E, p, arith, steps, warmup=3, keep=True):
+    """Device time (ms) of `steps` steps replayed from a captured graph, after
+    `warmup` steps and one untimed pass that captures the graph."""
+    old_keep = os.environ.get("E2D_KEEP_PRIMS")
+    os.environ["E2D_KEEP_PRIMS"] = "1" if keep else "0"
+    try:
+        with E.HydroRun(p, arith=arith) as r:
+            r.init_implode()
+            r.advance(0, warmup, log=False)
+            r.advance(warmup, steps, log=False)
+            r.advance(warmup + steps, steps, log=False)
+            return r.last_advance_ms()
+    finally:
+        if old_keep is None:
+            os.environ.pop("E2D_KEEP_PRIMS", None)
+        else:
+            os.environ["E2D_KEEP_PRIMS"] = old_keep
+
+
+def rel_l1(u, ref):
+    """Relative L1 difference per conservative variable (interior cells)."""
+    import numpy as np
+    u, ref = u[:, 2:-2, 2:-2].astype(np.float64), ref[:, 2:-2, 2:-2].astype(np.float64)
+    return {k: float(np.abs(u[v] - ref[v]).sum() / np.abs(ref[v]).sum())
+            for v, k in enumerate(("rho", "E", "rho_u", "rho_v"))}
+
+
 def run_ours(a, dist):
     import numpy as np
     import euler2d_cudafortran_gb300 as E
-    E.load_library()
+    E.load_library(a.arith)
     cells = a.nx * a.nx
+    riemann = E.RIEMANN_HLLC if a.riemann == "hllc" else E.RIEMANN_APPROX
     params = E.make_params(nx=a.nx, ny=a.nx, gamma0=1.4, cfl=0.8, implementation_version=a.version,
-                           riemann_solver=E.RIEMANN_HLLC if a.riemann == "hllc" else E.RIEMANN_APPROX,
-                           precision=a.precision)
-    run = E.HydroRun(params)
+                           riemann_solver=riemann, precision=a.precision)
+    run = E.HydroRun(params, arith=a.arith)
     run.init_implode()
     # warm-up: W steps (also builds and uploads the graphs)
     run.advance(0, a.warmup, log=False)
@@ -395,7 +447,7 @@ def run_ours(a, dist):
     hbm_peak, peak_kind = measured_peaks()
     bytes_per_launch = BYTES_PER_CELL[a.precision] * cells
     achieved = bytes_per_launch / (kern_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(a.precision, a.nx, a.version)
+    traffic = profiled_traffic(a.precision, a.nx, a.version, a.arith)
     dfma, ddiv = E.measure_fp64_peak()
     health = run.health()
     run.close()
@@ -411,10 +463,10 @@ def run_ours(a, dist):
         except Exception:
             host_u = np.empty((4, a.nx + 4, a.nx + 4), dtype=np.float64 if a.precision == 8 else np.float32)
             host_out = np.empty_like(host_u)
-        with E.HydroRun(params) as r2:
+        with E.HydroRun(params, arith=a.arith) as r2:
             r2.init_implode()
             host_u[...] = r2.get_state(0)
-        with E.HydroRun(params) as r2:
+        with E.HydroRun(params, arith=a.arith) as r2:
             # one untimed pass of the same sequence (graph-free path, kernels loaded)
             for rep in range(2):
                 dist.barrier()
@@ -438,8 +490,7 @@ def run_ours(a, dist):
                            "download final state"}
 
     # CPU baseline: single-thread restatement of serial_ref on a bounded sample
-    cpu = None
-    cpu_mc = None
+    cpu = cpu_mc = None
     if dist.rank == 0 and not a.no_cpu_baseline:
         from oracle import oracle as O
         O.build()
@@ -454,68 +505,92 @@ def run_ours(a, dist):
                   "kind": "port", "sample": f"{a.nx}x{a.nx}, {steps_mc} steps, OpenMP on the stdpar do-concurrent "
                                             "loops (stand-in for the unavailable -stdpar=multicore build)"}
 
+    # Every build against the FP64 oracle on the headline workload: the exact
+    # FP64 build bit for bit, the FMA FP64 build and both FP32 builds by
+    # relative L1 per variable and relative dt.
+    accuracy = None
+    if dist.rank == 0 and not a.no_variants and a.precision == 8:
+        from oracle import oracle as O
+        O.build()
+        po = oracle_params(a)
+        ref, dts_ref, _, _ = O.run(po, a.steps, prec="f64", nthreads=os.cpu_count() or 1)
+        accuracy = {"workload": f"{a.nx}x{a.nx}, {a.steps} steps, implementationVersion 0, against the FP64 oracle"}
+        for arith in ("exact", "fma"):
+            for prec in (8, 4):
+                p = E.make_params(nx=a.nx, ny=a.nx, gamma0=1.4, cfl=0.8, implementation_version=0,
+                                  riemann_solver=riemann, precision=prec)
+                u, dts = E.run_steps(a.steps, p, arith=arith)
+                dr = float(np.max(np.abs(dts.astype(np.float64) - dts_ref) / dts_ref))
+                key = f"{'fp64' if prec == 8 else 'fp32'}_{arith}"
+                row = {"rel_l1_per_variable": rel_l1(u, ref), "dt_max_rel": dr}
+                if prec == 8:
+                    row["bitwise"] = bool(np.array_equal(u[:, 2:-2, 2:-2], ref[:, 2:-2, 2:-2]) and
+                                          np.array_equal(dts, dts_ref))
+                    row["within_1e-12_l1_1e-14_dt"] = bool(max(row["rel_l1_per_variable"].values()) <= 1e-12
+                                                           and dr <= 1e-14)
+                accuracy[key] = row
+        del ref
+
     variants = None
     if dist.rank == 0 and not a.no_variants:
         variants = []
         # keep=False: implementationVersion 0 without the primitive arrays kept
         # beside the states (E2D_KEEP_PRIMS=0: every step converts its box, the
         # primitives never leave shared memory)
-        for (nx, prec, ver, keep) in ((2048, 8, 1, True), (2048, 8, 0, False), (2048, 4, 0, True), (2048, 4, 1, True),
-                                      (4096, 8, 0, True), (4096, 8, 1, True), (4096, 4, 0, True), (4096, 4, 1, True)):
+        rows = [(nx, prec, ver, True, ar) for ar in ("exact", "fma") for nx in (2048, 4096) for prec in (8, 4)
+                for ver in (0, 1)]
+        rows.insert(1, (2048, 8, 0, False, "exact"))
+        for (nx, prec, ver, keep, ar) in rows:
             p = E.make_params(nx=nx, ny=nx, gamma0=1.4, cfl=0.8, implementation_version=ver,
-                              riemann_solver=params.riemann_solver, precision=prec)
-            old_keep = os.environ.get("E2D_KEEP_PRIMS")
-            os.environ["E2D_KEEP_PRIMS"] = "1" if keep else "0"
-            try:
-                with E.HydroRun(p) as r3:
-                    r3.init_implode()
-                    ns = 20
-                    r3.advance(0, 3, log=False)
-                    r3.advance(3, ns, log=False)
-                    r3.advance(3 + ns, ns, log=False)
-                    vms = r3.last_advance_ms()
-            finally:
-                if old_keep is None:
-                    os.environ.pop("E2D_KEEP_PRIMS", None)
-                else:
-                    os.environ["E2D_KEEP_PRIMS"] = old_keep
+                              riemann_solver=riemann, precision=prec)
+            vms = time_run(E, p, ar, a.steps, keep=keep)
+            mc = nx * nx * a.steps / (vms * 1e-3) / 1e6
+            gbs = mc * 1e6 * BYTES_PER_CELL[prec] / 1e9
             row = {"nx": nx, "precision": "FP64" if prec == 8 else "FP32", "implementationVersion": ver,
-                   "steps": ns, "mcells_per_s": round(nx * nx * ns / (vms * 1e-3) / 1e6, 2)}
+                   "arith": ar, "steps": a.steps, "mcells_per_s": round(mc, 2),
+                   "hbm": {"bytes_per_cell": BYTES_PER_CELL[prec], "achieved_gbs": round(gbs, 1),
+                           "frac": round(gbs / hbm_peak, 5)}}
             if ver == 0:
                 row["primitives_kept"] = keep
+            inst = profiled_value(prec, nx, ver, "thread_inst_per_cell", ar)
+            if inst and prec == 4 and clk.get("sm_mhz"):
+                # FP32 is bound by instruction issue: 4 schedulers x 32 lanes per SM per clock
+                issue_peak = 152 * 4 * 32 * clk["sm_mhz"] * 1e6
+                row["binding_roof"] = {"roof": "instruction issue", "thread_inst_per_cell": inst,
+                                       "frac": round(inst * mc * 1e6 / issue_peak, 4),
+                                       "frac_of": "152 SMs x 4 schedulers x 32 lanes x the sampled SM clock"}
+            fp64_inst = profiled_value(prec, nx, ver, "fp64_warp_inst_per_launch", ar)
+            if fp64_inst and prec == 8:
+                inst_s = 32 * fp64_inst / (nx * nx) * mc * 1e6
+                row["binding_roof"] = {"roof": "fp64 pipe", "fp64_inst_per_cell": round(32 * fp64_inst / (nx * nx), 1),
+                                       "frac": round(inst_s / dfma, 4), "frac_of": "the live DFMA probe"}
             variants.append(row)
-
-    # FP32 against the FP64 oracle: the FP64 run is bitwise the oracle's, so
-    # its state after `steps` steps stands for it
-    fp32_error = None
-    if dist.rank == 0 and not a.no_variants:
-        finals = {}
-        for prec in (8, 4):
-            p = E.make_params(nx=a.nx, ny=a.nx, gamma0=1.4, cfl=0.8, implementation_version=0,
-                              riemann_solver=params.riemann_solver, precision=prec)
-            with E.HydroRun(p) as r4:
-                r4.init_implode()
-                dts4 = r4.advance(0, a.steps)
-                finals[prec] = (r4.final_state(a.steps)[:, 2:-2, 2:-2].astype(np.float64), dts4.astype(np.float64))
-        (u64, dt64), (u32, dt32) = finals[8], finals[4]
-        rel = [float(np.abs(u32[v] - u64[v]).sum() / np.abs(u64[v]).sum()) for v in range(4)]
-        fp32_error = {"workload": f"{a.nx}x{a.nx}, {a.steps} steps, implementationVersion 0",
-                      "rel_l1_per_variable": {"rho": rel[0], "E": rel[1], "rho_u": rel[2], "rho_v": rel[3]},
-                      "dt_max_rel": float(np.max(np.abs(dt32 - dt64) / dt64))}
 
     batched = None
     if dist.rank == 0 and not a.no_batched:
         batched = measure_batched(E, a)
-    adjoint = adjoint_batch = None
+        single = value / dist.ws
+        batched["ceiling"] = {
+            "single_run_mcells_per_s": round(single, 2),
+            "fraction_of_single_run": round(batched["mcells_per_s"] / single, 4),
+            "note": "both the ensemble and the single run are bound by the FP64 pipe, so the single run's rate on "
+                    "the largest grid is the ensemble's ceiling; batching can only recover the small-problem tail"}
+        if a.precision == 8:
+            inst = profiled_value(8, 2048, 0, "fp64_warp_inst_per_launch", a.arith)
+            if inst:
+                per_cell = 32 * inst / (2048 * 2048)
+                batched["ceiling"]["fp64_pipe_frac"] = round(per_cell * batched["mcells_per_s"] * 1e6 / dfma, 4)
+    adjoint = adjoint_ckpt = adjoint_batch = None
     if dist.rank == 0 and not a.no_adjoint:
-        adjoint = measure_adjoint(E, a)
+        adjoint = measure_adjoint(E, a, full_tape=True)
+        adjoint_ckpt = measure_adjoint(E, a, full_tape=False)
         if a.adjoint_batch_steps > 0:
             adjoint_batch = measure_adjoint_batch(E, a)
 
     fp64_roof = {"pipe": "fp64", "dfma_per_s": dfma, "ddiv_per_s": ddiv,
                  "note": "the FP64 step is bound by the FP64 pipe (two Riemann solves, traces, slopes per cell), "
                          "not by HBM"}
-    warp_inst = profiled_value(a.precision, a.nx, a.version, "fp64_warp_inst_per_launch")
+    warp_inst = profiled_value(a.precision, a.nx, a.version, "fp64_warp_inst_per_launch", a.arith)
     if warp_inst and a.precision == 8 and a.riemann == "hllc":
         inst_s = 32 * warp_inst / (kern_ms * 1e-3)  # FP64 thread instructions per second, this run
         fp64_roof.update({"fp64_inst_per_cell": round(32 * warp_inst / (a.nx * a.nx), 1),
@@ -528,10 +603,8 @@ def run_ours(a, dist):
             "n_gpus": dist.ws, "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms / a.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if a.precision == 8 else "f32", "data": "synthetic",
-            "config": {"workload": workload_name(a), "nx": a.nx, "ny": a.nx, "steps": a.steps,
-                       "parallelism": "replicas" if dist.ws > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (u and u2: 2 x %.1f MB ping-pong per step)"
-                             % (4 * isz * isz * a.precision / 1e6)},
+            "config": bench_config(a, dist.ws),
+            "arith": a.arith,
             "value_reference_formula": round(dist.ws * isz * isz * a.steps / (ms * 1e-3) / 1e6, 3),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(achieved / hbm_peak, 5), "peak_kind": peak_kind,
@@ -547,14 +620,14 @@ def run_ours(a, dist):
             "gpu_launches": (a.steps + 1 + (0 if os.environ.get("E2D_KEEP_PRIMS") == "0" else 2)
                              if a.version == 0 else 4 * a.steps),
             "health_flags": health,
+            "accuracy_vs_fp64_oracle": accuracy,
             "variants": variants,
-            "fp32_error_vs_fp64_oracle": fp32_error,
             "batched": batched,
             "adjoint": adjoint,
+            "adjoint_checkpointed": adjoint_ckpt,
             "adjoint_batched": adjoint_batch,
         }
         print(json.dumps(line), flush=True)
-
 
 def main():
     a = parse_args()

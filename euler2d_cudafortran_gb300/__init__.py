@@ -18,6 +18,12 @@ run_cleanup :172                       ``HydroRun.close()``
 
 There is no CPU fallback: every call runs the CUDA library, and importing the
 wrapper fails loudly if the library was not built.
+
+Two builds of the library share the C ABI (``e2d_arithmetic``): ``"exact"``
+(``libeuler2d_gb300.so``, no multiply-add contraction, bitwise serial_ref
+arithmetic) and ``"fma"`` (``libeuler2d_gb300_fma.so``, multiply-adds fused).
+Every class takes ``arith=`` to pick one; the default is ``"exact"``, or the
+value of the environment variable ``E2D_ARITH``.
 """
 from __future__ import annotations
 
@@ -26,10 +32,12 @@ import os
 
 import numpy as np
 
+from .build import LIBS as LIB_PATHS
 from .namelist import RunConfig, read_config  # noqa: F401
 
-_HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_build", "libeuler2d_gb300.so")
+LIB_PATH = LIB_PATHS["exact"]
+ARITH_EXACT = 0
+ARITH_FMA = 1
 
 E2D_OK = 0
 E2D_ERR_INVALID_ARG = 1
@@ -44,7 +52,7 @@ RIEMANN_APPROX = 0
 RIEMANN_HLLC = 2
 
 EXPORTED_SYMBOLS = [
-    "e2d_default_params", "e2d_create", "e2d_destroy", "e2d_get_sizes", "e2d_set_stream", "e2d_synchronize",
+    "e2d_default_params", "e2d_arithmetic", "e2d_create", "e2d_destroy", "e2d_get_sizes", "e2d_set_stream", "e2d_synchronize",
     "e2d_init_implode", "e2d_init_diagonal", "e2d_upload_state", "e2d_download_state", "e2d_compute_dt",
     "e2d_make_boundaries", "e2d_godunov_unsplit", "e2d_advance", "e2d_last_advance_ms", "e2d_get_invdt",
     "e2d_get_health", "e2d_last_error", "e2d_device_state", "e2d_time_steps", "e2d_measure_fp64_peak",
@@ -82,14 +90,25 @@ class Params(ctypes.Structure):
     ]
 
 
-_lib = None
+_libs: dict = {}
 
 
-def load_library(path: str = LIB_PATH):
-    """Load the CUDA library (raises if it has not been built)."""
-    global _lib
-    if _lib is not None:
-        return _lib
+def default_arith() -> str:
+    a = os.environ.get("E2D_ARITH", "exact")
+    if a not in LIB_PATHS:
+        raise ValueError(f"E2D_ARITH must be one of {sorted(LIB_PATHS)}, not {a!r}")
+    return a
+
+
+def load_library(arith: str | None = None):
+    """Load one build of the CUDA library, "exact" or "fma" (raises if it has
+    not been built)."""
+    arith = arith or default_arith()
+    if arith in _libs:
+        return _libs[arith]
+    if arith not in LIB_PATHS:
+        raise ValueError(f"arith must be one of {sorted(LIB_PATHS)}, not {arith!r}")
+    path = LIB_PATHS[arith]
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build it with `python -m euler2d_cudafortran_gb300.build` "
                           "(there is no CPU fallback)")
@@ -97,6 +116,7 @@ def load_library(path: str = LIB_PATH):
     vp, ip, i, d = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_double
     sig = {
         "e2d_default_params": [ctypes.POINTER(Params)],
+        "e2d_arithmetic": [ip],
         "e2d_create": [ctypes.POINTER(Params), ctypes.POINTER(vp)],
         "e2d_destroy": [vp],
         "e2d_get_sizes": [vp, ip, ip, ctypes.POINTER(ctypes.c_size_t)],
@@ -117,7 +137,8 @@ def load_library(path: str = LIB_PATH):
         "e2d_get_health": [vp, ctypes.POINTER(ctypes.c_uint)],
         "e2d_device_state": [vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t),
                              ctypes.POINTER(ctypes.c_size_t)],
-        "e2d_godunov_unsplit_noalloc": [ctypes.POINTER(Params), vp, vp, ctypes.c_size_t, d, vp],
+        "e2d_godunov_unsplit_noalloc": [ctypes.POINTER(Params), vp, vp, ctypes.c_size_t, d, vp,
+                                        ctypes.POINTER(ctypes.c_uint)],
         "e2d_selftest_wait": [ctypes.c_longlong, ip, ip, ctypes.POINTER(ctypes.c_longlong)],
         "e2d_begin_download": [vp, i, vp],
         "e2d_wait_download": [vp],
@@ -160,13 +181,26 @@ def load_library(path: str = LIB_PATH):
         fn.restype = ctypes.c_int
     lib.e2d_last_error.argtypes = []
     lib.e2d_last_error.restype = ctypes.c_char_p
-    _lib = lib
+    mode = ctypes.c_int(-1)
+    lib.e2d_arithmetic(ctypes.byref(mode))
+    if mode.value != {"exact": ARITH_EXACT, "fma": ARITH_FMA}[arith]:
+        raise ImportError(f"{path} reports arithmetic {mode.value}, not {arith}")
+    _libs[arith] = lib
     return lib
 
 
-def _check(rc: int):
+def _check(rc: int, lib=None):
     if rc != E2D_OK:
-        raise E2DError(rc, load_library().e2d_last_error().decode())
+        raise E2DError(rc, (lib or load_library()).e2d_last_error().decode())
+
+
+class _Handle:
+    """Base of the run classes: errors are read from the library build that
+    returned them."""
+    _lib = None
+
+    def _ok(self, rc: int):
+        _check(rc, self._lib)
 
 
 def default_params() -> Params:
@@ -194,17 +228,17 @@ def make_params(**kw) -> Params:
     return p
 
 
-class HydroRun:
+class HydroRun(_Handle):
     """One run on the current CUDA device: u, u2 and the step's work arrays."""
 
-    def __init__(self, params: Params | None = None, **kw):
-        self._lib = load_library()
+    def __init__(self, params: Params | None = None, arith: str | None = None, **kw):
+        self._lib = load_library(arith)
         self.params = params if params is not None else make_params(**kw)
         h = ctypes.c_void_p()
-        _check(self._lib.e2d_create(ctypes.byref(self.params), ctypes.byref(h)))
+        self._ok(self._lib.e2d_create(ctypes.byref(self.params), ctypes.byref(h)))
         self._h = h
         isz, jsz, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
-        _check(self._lib.e2d_get_sizes(h, ctypes.byref(isz), ctypes.byref(jsz), ctypes.byref(nb)))
+        self._ok(self._lib.e2d_get_sizes(h, ctypes.byref(isz), ctypes.byref(jsz), ctypes.byref(nb)))
         self.isize, self.jsize, self.state_bytes = isz.value, jsz.value, nb.value
         self.dtype = np.float64 if self.params.precision == 8 else np.float32
 
@@ -231,16 +265,16 @@ class HydroRun:
         return np.zeros((4, self.jsize, self.isize), dtype=self.dtype)
 
     def init_implode(self):
-        _check(self._lib.e2d_init_implode(self._h))
+        self._ok(self._lib.e2d_init_implode(self._h))
 
     def init_diagonal(self, offset, rho_hi, p_hi, rho_lo, p_lo):
-        _check(self._lib.e2d_init_diagonal(self._h, offset, rho_hi, p_hi, rho_lo, p_lo))
+        self._ok(self._lib.e2d_init_diagonal(self._h, offset, rho_hi, p_hi, rho_lo, p_lo))
 
     def set_state(self, which: int, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=self.dtype)
         if a.shape != (4, self.jsize, self.isize):
             raise ValueError(f"state must have shape (4, {self.jsize}, {self.isize})")
-        _check(self._lib.e2d_upload_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
+        self._ok(self._lib.e2d_upload_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
 
     def get_state(self, which: int, out: np.ndarray | None = None) -> np.ndarray:
         """State `which` (0 = u, 1 = u2) in Fortran layout; into `out` (e.g. a
@@ -251,7 +285,7 @@ class HydroRun:
             if out.shape != (4, self.jsize, self.isize) or out.dtype != self.dtype or not out.flags["C_CONTIGUOUS"]:
                 raise ValueError("out must be a C-contiguous state array of this run")
             a = out
-        _check(self._lib.e2d_download_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
+        self._ok(self._lib.e2d_download_state(self._h, which, a.ctypes.data_as(ctypes.c_void_p)))
         return a
 
     def begin_download(self, which: int, out: np.ndarray):
@@ -260,57 +294,57 @@ class HydroRun:
         if out.shape != (4, self.jsize, self.isize) or out.dtype != self.dtype or not out.flags["C_CONTIGUOUS"]:
             raise ValueError("out must be a C-contiguous state array of this run")
         self._pending_out = out
-        _check(self._lib.e2d_begin_download(self._h, which, out.ctypes.data_as(ctypes.c_void_p)))
+        self._ok(self._lib.e2d_begin_download(self._h, which, out.ctypes.data_as(ctypes.c_void_p)))
 
     def wait_download(self) -> np.ndarray | None:
-        _check(self._lib.e2d_wait_download(self._h))
+        self._ok(self._lib.e2d_wait_download(self._h))
         out, self._pending_out = getattr(self, "_pending_out", None), None
         return out
 
     # -- the reference procedures -----------------------------------------
     def compute_dt(self, useU: int) -> float:
         dt = (ctypes.c_double if self.params.precision == 8 else ctypes.c_float)()
-        _check(self._lib.e2d_compute_dt(self._h, useU, ctypes.byref(dt)))
+        self._ok(self._lib.e2d_compute_dt(self._h, useU, ctypes.byref(dt)))
         return dt.value
 
     def make_boundaries(self, which: int):
-        _check(self._lib.e2d_make_boundaries(self._h, which))
+        self._ok(self._lib.e2d_make_boundaries(self._h, which))
 
     def godunov_unsplit(self, nStep: int, dt: float):
-        _check(self._lib.e2d_godunov_unsplit(self._h, nStep, float(dt)))
+        self._ok(self._lib.e2d_godunov_unsplit(self._h, nStep, float(dt)))
 
     def advance(self, nStep0: int, nsteps: int, log: bool = True):
         buf = np.zeros(max(nsteps, 1), dtype=self.dtype) if log else None
         ptr = buf.ctypes.data_as(ctypes.c_void_p) if log else None
-        _check(self._lib.e2d_advance(self._h, nStep0, nsteps, ptr))
+        self._ok(self._lib.e2d_advance(self._h, nStep0, nsteps, ptr))
         return buf[:nsteps] if log else None
 
     def last_advance_ms(self) -> float:
         ms = ctypes.c_float()
-        _check(self._lib.e2d_last_advance_ms(self._h, ctypes.byref(ms)))
+        self._ok(self._lib.e2d_last_advance_ms(self._h, ctypes.byref(ms)))
         return ms.value
 
     def time_steps(self, nStep0: int, nsteps: int) -> np.ndarray:
         """Per-step device time (ms) of nsteps steps launched one by one."""
         ms = np.zeros(nsteps, dtype=np.float32)
-        _check(self._lib.e2d_time_steps(self._h, nStep0, nsteps,
+        self._ok(self._lib.e2d_time_steps(self._h, nStep0, nsteps,
                                         ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
         return ms
 
     def synchronize(self):
-        _check(self._lib.e2d_synchronize(self._h))
+        self._ok(self._lib.e2d_synchronize(self._h))
 
     def set_stream(self, stream_ptr: int | None):
-        _check(self._lib.e2d_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+        self._ok(self._lib.e2d_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 
     def invdt(self) -> float:
         x = ctypes.c_double()
-        _check(self._lib.e2d_get_invdt(self._h, ctypes.byref(x)))
+        self._ok(self._lib.e2d_get_invdt(self._h, ctypes.byref(x)))
         return x.value
 
     def health(self) -> int:
         x = ctypes.c_uint()
-        _check(self._lib.e2d_get_health(self._h, ctypes.byref(x)))
+        self._ok(self._lib.e2d_get_health(self._h, ctypes.byref(x)))
         return x.value
 
     def final_state(self, nsteps: int) -> np.ndarray:
@@ -318,11 +352,11 @@ class HydroRun:
         return self.get_state(nsteps % 2)
 
 
-class Batch:
+class Batch(_Handle):
     """An ensemble of independent runs advanced together (e2d_batch_*)."""
 
-    def __init__(self, sizes, bcs=None, params: Params | None = None, **kw):
-        self._lib = load_library()
+    def __init__(self, sizes, bcs=None, params: Params | None = None, arith: str | None = None, **kw):
+        self._lib = load_library(arith)
         self.params = params if params is not None else make_params(**kw)
         self.sizes = [(int(a), int(b)) for a, b in sizes]
         n = len(self.sizes)
@@ -333,7 +367,7 @@ class Batch:
             flat = [int(x) for row in bcs for x in (row if hasattr(row, "__len__") else (row,) * 4)]
             bc = (ctypes.c_int * len(flat))(*flat)
         h = ctypes.c_void_p()
-        _check(self._lib.e2d_batch_create(ctypes.byref(self.params), n, nx, ny, bc, ctypes.byref(h)))
+        self._ok(self._lib.e2d_batch_create(ctypes.byref(self.params), n, nx, ny, bc, ctypes.byref(h)))
         self._h = h
         self.nprob = n
         self.dtype = np.float64 if self.params.precision == 8 else np.float32
@@ -359,64 +393,64 @@ class Batch:
         arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (self.nprob,)))
                 for x in (offset, rho_hi, p_hi, rho_lo, p_lo)]
         ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrs]
-        _check(self._lib.e2d_batch_init_diagonal(self._h, *ptrs))
+        self._ok(self._lib.e2d_batch_init_diagonal(self._h, *ptrs))
 
     def get_state(self, prob: int, which: int) -> np.ndarray:
         nx, ny = self.sizes[prob]
         a = np.zeros((4, ny + 4, nx + 4), dtype=self.dtype)
-        _check(self._lib.e2d_batch_download_state(self._h, prob, which, a.ctypes.data_as(ctypes.c_void_p)))
+        self._ok(self._lib.e2d_batch_download_state(self._h, prob, which, a.ctypes.data_as(ctypes.c_void_p)))
         return a
 
     def set_state(self, prob: int, which: int, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=self.dtype)
-        _check(self._lib.e2d_batch_upload_state(self._h, prob, which, a.ctypes.data_as(ctypes.c_void_p)))
+        self._ok(self._lib.e2d_batch_upload_state(self._h, prob, which, a.ctypes.data_as(ctypes.c_void_p)))
 
     def advance(self, nStep0: int, nsteps: int, log: bool = True):
         buf = np.zeros((max(nsteps, 1), self.nprob), dtype=self.dtype) if log else None
-        _check(self._lib.e2d_batch_advance(self._h, nStep0, nsteps,
+        self._ok(self._lib.e2d_batch_advance(self._h, nStep0, nsteps,
                                            buf.ctypes.data_as(ctypes.c_void_p) if log else None))
         return buf[:nsteps] if log else None
 
     def last_advance_ms(self) -> float:
         ms = ctypes.c_float()
-        _check(self._lib.e2d_batch_last_advance_ms(self._h, ctypes.byref(ms)))
+        self._ok(self._lib.e2d_batch_last_advance_ms(self._h, ctypes.byref(ms)))
         return ms.value
 
     def set_schedule(self, variant: int, grid_mult: int, order: int):
-        _check(self._lib.e2d_batch_set_schedule(self._h, variant, grid_mult, order))
+        self._ok(self._lib.e2d_batch_set_schedule(self._h, variant, grid_mult, order))
 
     def schedule(self):
         v, m, o, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        _check(self._lib.e2d_batch_get_schedule(self._h, ctypes.byref(v), ctypes.byref(m), ctypes.byref(o),
+        self._ok(self._lib.e2d_batch_get_schedule(self._h, ctypes.byref(v), ctypes.byref(m), ctypes.byref(o),
                                                 ctypes.byref(g)))
         return {"tile": ["32x15", "32x7"][v.value], "variant": v.value, "grid_mult": m.value,
                 "order": ["problem", "largest-first"][o.value], "grid": g.value}
 
     def tune(self, steps: int = 3, cache_path: str | None = None) -> float:
         ms = ctypes.c_float()
-        _check(self._lib.e2d_batch_tune(self._h, steps, cache_path.encode() if cache_path else None,
+        self._ok(self._lib.e2d_batch_tune(self._h, steps, cache_path.encode() if cache_path else None,
                                         ctypes.byref(ms)))
         return ms.value
 
     def health(self, prob: int) -> int:
         x = ctypes.c_uint()
-        _check(self._lib.e2d_batch_get_health(self._h, prob, ctypes.byref(x)))
+        self._ok(self._lib.e2d_batch_get_health(self._h, prob, ctypes.byref(x)))
         return x.value
 
     def final_state(self, prob: int, nsteps: int) -> np.ndarray:
         return self.get_state(prob, nsteps % 2)
 
 
-class Adjoint:
+class Adjoint(_Handle):
     """Discrete adjoint of the FP64 HLLC step: J = sum rho^2 w(x, y) after
     nsteps steps and dJ/d(initial interior density) (e2d_adjoint_*)."""
 
-    def __init__(self, params: Params | None = None, **kw):
-        self._lib = load_library()
+    def __init__(self, params: Params | None = None, arith: str | None = None, **kw):
+        self._lib = load_library(arith)
         kw.setdefault("riemann_solver", RIEMANN_HLLC)
         self.params = params if params is not None else make_params(**kw)
         h = ctypes.c_void_p()
-        _check(self._lib.e2d_adjoint_create(ctypes.byref(self.params), ctypes.byref(h)))
+        self._ok(self._lib.e2d_adjoint_create(ctypes.byref(self.params), ctypes.byref(h)))
         self._h = h
         self.nx, self.ny = self.params.nx, self.params.ny
 
@@ -451,7 +485,7 @@ class Adjoint:
         if dt_fixed is not None:
             dtf = np.ascontiguousarray(dt_fixed, dtype=np.float64)
             dtp = dtf.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        _check(self._lib.e2d_adjoint_objective(self._h, ptr, nsteps, xc, yc, sigma, dtp, ctypes.byref(J)))
+        self._ok(self._lib.e2d_adjoint_objective(self._h, ptr, nsteps, xc, yc, sigma, dtp, ctypes.byref(J)))
         return J.value
 
     def gradient(self, nsteps, u0=None, dt_mode=1, xc=0.6, yc=0.6, sigma=0.1):
@@ -460,31 +494,31 @@ class Adjoint:
         J = ctypes.c_double()
         g = np.zeros((self.ny, self.nx), dtype=np.float64)
         dts = np.zeros(nsteps, dtype=np.float64)
-        _check(self._lib.e2d_adjoint_gradient(self._h, ptr, nsteps, dt_mode, xc, yc, sigma, ctypes.byref(J),
+        self._ok(self._lib.e2d_adjoint_gradient(self._h, ptr, nsteps, dt_mode, xc, yc, sigma, ctypes.byref(J),
                                               g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                               dts.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return J.value, g, dts
 
     def last_ms(self):
         a, b = ctypes.c_float(), ctypes.c_float()
-        _check(self._lib.e2d_adjoint_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
+        self._ok(self._lib.e2d_adjoint_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
     def layout(self):
         """(steps between checkpoints, tape in use) of the last gradient call;
         the first equals the step count when every state and tape were kept."""
         k, t = ctypes.c_int(), ctypes.c_int()
-        _check(self._lib.e2d_adjoint_layout(self._h, ctypes.byref(k), ctypes.byref(t)))
+        self._ok(self._lib.e2d_adjoint_layout(self._h, ctypes.byref(k), ctypes.byref(t)))
         return k.value, bool(t.value)
 
 
-class AdjointBatch:
+class AdjointBatch(_Handle):
     """The discrete adjoint of an ensemble of FP64 HLLC problems of uneven
     sizes, all stages batched, one captured graph per call
     (e2d_adjoint_batch_*)."""
 
-    def __init__(self, sizes, bcs=None, params: Params | None = None, **kw):
-        self._lib = load_library()
+    def __init__(self, sizes, bcs=None, params: Params | None = None, arith: str | None = None, **kw):
+        self._lib = load_library(arith)
         kw.setdefault("riemann_solver", RIEMANN_HLLC)
         self.params = params if params is not None else make_params(**kw)
         self.sizes = [(int(a), int(b)) for a, b in sizes]
@@ -496,7 +530,7 @@ class AdjointBatch:
             flat = [int(x) for row in bcs for x in (row if hasattr(row, "__len__") else (row,) * 4)]
             bc = (ctypes.c_int * len(flat))(*flat)
         h = ctypes.c_void_p()
-        _check(self._lib.e2d_adjoint_batch_create(ctypes.byref(self.params), n, nx, ny, bc, ctypes.byref(h)))
+        self._ok(self._lib.e2d_adjoint_batch_create(ctypes.byref(self.params), n, nx, ny, bc, ctypes.byref(h)))
         self._h = h
         self.nprob = n
 
@@ -521,18 +555,18 @@ class AdjointBatch:
         arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (self.nprob,)))
                 for x in (offset, rho_hi, p_hi, rho_lo, p_lo)]
         ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrs]
-        _check(self._lib.e2d_adjoint_batch_init_diagonal(self._h, *ptrs))
+        self._ok(self._lib.e2d_adjoint_batch_init_diagonal(self._h, *ptrs))
 
     def set_state(self, prob, u0):
         a = np.ascontiguousarray(u0, dtype=np.float64)
         nx, ny = self.sizes[prob]
         if a.shape != (4, ny + 4, nx + 4):
             raise ValueError(f"state of problem {prob} must have shape {(4, ny + 4, nx + 4)}")
-        _check(self._lib.e2d_adjoint_batch_upload_state(self._h, prob, a.ctypes.data_as(ctypes.c_void_p)))
+        self._ok(self._lib.e2d_adjoint_batch_upload_state(self._h, prob, a.ctypes.data_as(ctypes.c_void_p)))
 
     def objective(self, nsteps, xc=0.6, yc=0.6, sigma=0.1):
         J = np.zeros(self.nprob)
-        _check(self._lib.e2d_adjoint_batch_objective(self._h, nsteps, xc, yc, sigma,
+        self._ok(self._lib.e2d_adjoint_batch_objective(self._h, nsteps, xc, yc, sigma,
                                                      J.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return J
 
@@ -542,7 +576,7 @@ class AdjointBatch:
         g = np.zeros(sum(a * b for a, b in self.sizes))
         dts = np.zeros((nsteps, self.nprob))
         dp = ctypes.POINTER(ctypes.c_double)
-        _check(self._lib.e2d_adjoint_batch_gradient(self._h, nsteps, dt_mode, xc, yc, sigma, J.ctypes.data_as(dp),
+        self._ok(self._lib.e2d_adjoint_batch_gradient(self._h, nsteps, dt_mode, xc, yc, sigma, J.ctypes.data_as(dp),
                                                     g.ctypes.data_as(dp), dts.ctypes.data_as(dp)))
         grads, o = [], 0
         for nx, ny in self.sizes:
@@ -552,7 +586,7 @@ class AdjointBatch:
 
     def last_ms(self):
         a, b = ctypes.c_float(), ctypes.c_float()
-        _check(self._lib.e2d_adjoint_batch_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
+        self._ok(self._lib.e2d_adjoint_batch_last_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
 
@@ -561,6 +595,14 @@ def measure_fp64_peak():
     a, b = ctypes.c_double(), ctypes.c_double()
     _check(load_library().e2d_measure_fp64_peak(ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+def arithmetic(arith: str | None = None) -> int:
+    """ARITH_EXACT or ARITH_FMA, as the loaded build reports it."""
+    lib = load_library(arith)
+    m = ctypes.c_int()
+    _check(lib.e2d_arithmetic(ctypes.byref(m)), lib)
+    return m.value
 
 
 def selftest_wait(limit_cycles: int = 1 << 24):

@@ -13,6 +13,7 @@
 #include "../../include/euler2d_gb300.h"
 #include "hydro_params.h"
 #include "launch.h"
+#include "nvtx_ranges.h"
 
 using namespace e2d;
 
@@ -122,7 +123,10 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
   sd.dt_log = from_slot ? static_cast<Real*>(r->dt_log) : nullptr;
   sd.log_index = log_index;
   cudaStream_t s = r->stream;
-  if (!boundaries_done) launch_boundaries<Real>(h, in, s);
+  if (!boundaries_done) {
+    NvtxRange rg(NVTX_BOUNDARIES);
+    launch_boundaries<Real>(h, in, s);
+  }
   switch (r->p.implementation_version) {
     case 0: {
       // In the advance path the ghost cells of `out` are written by the
@@ -133,8 +137,14 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
       break;
     }
     case 1: {
+      // the reference's stages: primitives, then the traces and fluxes of
+      // computeAndStoreFluxes, then (here fused with them) updateHydro
       Field<Real> q = field<Real>(r, r->work[0]);
-      launch_prim<Real>(h, in, q, s);
+      {
+        NvtxRange rg(NVTX_PRIMITIVES);
+        launch_prim<Real>(h, in, q, s);
+      }
+      NvtxRange rg(NVTX_FLUXES);
       launch_trace_v1<Real>(h, q, sd, r->ctl, field<Real>(r, r->work[1]), field<Real>(r, r->work[2]),
                             field<Real>(r, r->work[3]), field<Real>(r, r->work[4]), s);
       launch_flux_update_v1<Real>(h, in, field<Real>(r, r->work[1]), field<Real>(r, r->work[2]),
@@ -143,8 +153,15 @@ void enqueue_step(e2d_run* r, int nStep, Real dt_value, bool from_slot, int rd, 
     }
     default: {
       Field<Real> q = field<Real>(r, r->work[0]);
-      launch_prim<Real>(h, in, q, s);
-      launch_fluxes_v2<Real>(h, q, sd, r->ctl, field<Real>(r, r->work[1]), field<Real>(r, r->work[2]), s);
+      {
+        NvtxRange rg(NVTX_PRIMITIVES);
+        launch_prim<Real>(h, in, q, s);
+      }
+      {
+        NvtxRange rg(NVTX_FLUXES);
+        launch_fluxes_v2<Real>(h, q, sd, r->ctl, field<Real>(r, r->work[1]), field<Real>(r, r->work[2]), s);
+      }
+      NvtxRange rg(NVTX_UPDATE);
       launch_update_v2<Real>(h, in, field<Real>(r, r->work[1]), field<Real>(r, r->work[2]), out, sd, r->ctl, s);
       break;
     }
@@ -192,9 +209,15 @@ template <typename Real>
 void enqueue_percall_q(e2d_run* r, int nStep, Real dt) {
   const Hydro<Real>& h = hydro<Real>(r);
   const int b = nStep % 2;
-  launch_boundaries<Real>(h, field<Real>(r, b ? r->u2 : r->u), r->stream);
-  if (r->q_valid[b]) launch_boundaries<Real>(h, field<Real>(r, r->qprim[b]), r->stream);
-  else refresh_prims<Real>(r, nStep);
+  {
+    NvtxRange rg(NVTX_BOUNDARIES);
+    launch_boundaries<Real>(h, field<Real>(r, b ? r->u2 : r->u), r->stream);
+    if (r->q_valid[b]) launch_boundaries<Real>(h, field<Real>(r, r->qprim[b]), r->stream);
+  }
+  if (!r->q_valid[b]) {
+    NvtxRange rg(NVTX_PRIMITIVES);
+    refresh_prims<Real>(r, nStep);
+  }
   enqueue_step<Real>(r, nStep, dt, false, -1, r->cur_slot, 0, true, true);
   r->q_valid[0] = r->q_valid[1] = true;
 }
@@ -248,6 +271,16 @@ int e2d_default_params(e2d_params* p) {
   p->implementation_version = 0;
   p->riemann_solver = E2D_RIEMANN_APPROX;
   p->precision = 8;
+  return E2D_OK;
+}
+
+int e2d_arithmetic(int* mode) {
+  if (!mode) return fail(E2D_ERR_INVALID_ARG, "null argument");
+#if defined(E2D_FMA) && E2D_FMA
+  *mode = E2D_ARITH_FMA;
+#else
+  *mode = E2D_ARITH_EXACT;
+#endif
   return E2D_OK;
 }
 
@@ -487,6 +520,7 @@ int e2d_host_free(void* ptr) {
 }
 
 int e2d_compute_dt(e2d_run* r, int useU, void* dt) {
+  NvtxRange rg(NVTX_COMPUTE_DT);
   if (int rc = check_run(r)) return rc;
   if (!dt || (useU != 0 && useU != 1)) return fail(E2D_ERR_INVALID_ARG, "bad compute_dt arguments");
   if (int rc = use_device(r)) return rc;
@@ -504,6 +538,7 @@ int e2d_compute_dt(e2d_run* r, int useU, void* dt) {
 }
 
 int e2d_make_boundaries(e2d_run* r, int which) {
+  NvtxRange rg(NVTX_BOUNDARIES);
   if (int rc = check_run(r)) return rc;
   if (which != 0 && which != 1) return fail(E2D_ERR_INVALID_ARG, "which must be 0 (u) or 1 (u2)");
   if (int rc = use_device(r)) return rc;
@@ -519,6 +554,7 @@ int e2d_make_boundaries(e2d_run* r, int which) {
 
 
 int e2d_godunov_unsplit(e2d_run* r, int nStep, double dt) {
+  NvtxRange rg(NVTX_GODUNOV);
   if (int rc = check_run(r)) return rc;
   if (nStep < 0) return fail(E2D_ERR_INVALID_ARG, "nStep must be >= 0");
   if (int rc = use_device(r)) return rc;
@@ -538,6 +574,7 @@ int e2d_godunov_unsplit(e2d_run* r, int nStep, double dt) {
 }
 
 int e2d_advance(e2d_run* r, int nStep0, int nsteps, void* dt_log) {
+  NvtxRange rg(NVTX_GODUNOV);  // nsteps steps: compute_dt and godunov_unsplit each, one graph
   if (int rc = check_run(r)) return rc;
   if (nStep0 < 0 || nsteps < 0) return fail(E2D_ERR_INVALID_ARG, "nStep0 and nsteps must be >= 0");
   if (int rc = use_device(r)) return rc;

@@ -68,6 +68,18 @@ typedef struct e2d_run e2d_run; /* opaque run handle: owns u, u2 and work arrays
  * implementationVersion 0, approximate Riemann solver. */
 int e2d_default_params(e2d_params* p);
 
+/* Arithmetic of this build of the library.  Two builds share this ABI:
+ * libeuler2d_gb300.so (E2D_ARITH_EXACT: no multiply-add contraction, every
+ * operation rounded as serial_ref's gfortran build rounds it, results bitwise
+ * those of serial_ref's arithmetic) and libeuler2d_gb300_fma.so
+ * (E2D_ARITH_FMA: multiply-adds fused, as nvfortran's default -O3 GPU builds
+ * of cuf/ and stdpar/ do -- cuf/Makefile:22, stdpar/Makefile:8 --, results
+ * within 1e-12 relative L1 and dt within 1e-14 of the exact build).  A host
+ * picks one at link time (-leuler2d_gb300 or -leuler2d_gb300_fma). */
+#define E2D_ARITH_EXACT 0
+#define E2D_ARITH_FMA 1
+int e2d_arithmetic(int* mode);
+
 /* initHydroParameters + run_init allocation (serial_ref/m_run.f90:48-128,150-158;
  * cuf/m_HydroRun_gpu.cuf:83-118).  Validates p, allocates u, u2 (zeroed, as fresh
  * allocate() pages) and the work arrays of the chosen implementation version on
@@ -276,18 +288,22 @@ int e2d_adjoint_batch_last_ms(e2d_adjoint_batch* b, float* objective_ms, float* 
  * by another allocator or memory pool, or a host framework that forbids
  * allocation on its time-step path).  u_in and u_out are device arrays in the
  * pitched layout of e2d_device_state (4 planes of ny+4 rows of pitch_elems
- * elements); make_boundaries is applied to u_in first, as the reference does.
- * The work arrays live in one static device array of
+ * elements, nx+4 <= pitch_elems <= INT_MAX), owned by the caller, that must
+ * not overlap; make_boundaries is applied to u_in first, as the reference
+ * does, and only the interior of u_out is written.  dt must be positive and
+ * finite.  The work arrays live in one static device array of
  * E2D_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
  * exit; grids whose three work arrays (primitives and two flux arrays) do not
  * fit are rejected with E2D_ERR_INVALID_ARG.  All calls share that array:
- * calls that overlap on the GPU race.  The first call on a device looks up
- * the array's device address and should come before any stream capture.
- * Work is issued on `stream` (a cudaStream_t, NULL = legacy default stream)
- * and not synchronised. */
+ * calls that overlap on the GPU race.  The first call on a device (and the
+ * first after a device reset) looks up the array's device address and should
+ * come before any stream capture.  Work is issued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) and not synchronised, unless
+ * `health` is not NULL: the call then waits for the step and stores its
+ * E2D_HEALTH_* flags there. */
 #define E2D_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
 int e2d_godunov_unsplit_noalloc(const e2d_params* p, void* u_in, void* u_out, size_t pitch_elems, double dt,
-                                void* stream);
+                                void* stream, unsigned* health);
 
 #ifdef __cplusplus
 }

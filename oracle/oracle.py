@@ -12,13 +12,14 @@ from __future__ import annotations
 
 import ctypes
 import os
+import platform
 import subprocess
 from dataclasses import dataclass
 
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_LIB_PATH = os.path.join(_HERE, "_build", platform.machine() or "unknown", "liboracle.so")
 _lib = None
 
 

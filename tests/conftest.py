@@ -27,7 +27,7 @@ def e2d():
     """The CUDA library wrapper; builds the library when it is missing."""
     import euler2d_cudafortran_gb300 as E
     from euler2d_cudafortran_gb300 import build
-    if not os.path.exists(E.LIB_PATH):
+    if not all(os.path.exists(p) for p in E.LIB_PATHS.values()):
         build.build()
     E.load_library()
     return E

@@ -24,11 +24,21 @@ def test_header_declares_the_boundary():
         assert n in names
 
 
-def test_library_exports_every_declared_symbol(e2d):
-    lib = ctypes.CDLL(e2d.LIB_PATH)
+@pytest.mark.parametrize("arith", ["exact", "fma"])
+def test_library_exports_every_declared_symbol(e2d, arith):
+    lib = ctypes.CDLL(e2d.LIB_PATHS[arith])
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, f"missing exports: {missing}"
     assert sorted(e2d.EXPORTED_SYMBOLS) == declared_functions()
+
+
+def test_each_build_reports_its_arithmetic(e2d):
+    """e2d_arithmetic needs no device: the exact and the FMA builds say which
+    they are, and load_library refuses a file that says otherwise."""
+    assert e2d.arithmetic("exact") == e2d.ARITH_EXACT
+    assert e2d.arithmetic("fma") == e2d.ARITH_FMA
+    lib = e2d.load_library("exact")
+    assert lib.e2d_arithmetic(None) == e2d.E2D_ERR_INVALID_ARG
 
 
 def test_params_struct_layout_matches_header(e2d, tmp_path):
