@@ -9,6 +9,12 @@ reference's HydroRun loop (compute_dt + godunov_unsplit) over the whole grid.
 Metric: Mcell-updates/s = nx * ny * steps / time (interior cells; the
 reference's own formula, which counts ghost cells, is reported beside it).
 
+Library build (--arith): "fma" (default; multiply-adds fused as nvfortran's
+GPU builds of the reference do, results within the specified 1e-12 relative
+L1 per variable and 1e-14 relative dt of the FP64 oracle, checked in the
+line's `accuracy_vs_fp64_oracle`) or "exact" (no contraction, bitwise the
+oracle).  Both builds appear in `variants`.
+
 value       device time (CUDA events on the launching stream) of `steps`
             steps replayed from a CUDA graph, state resident in HBM.
 e2e         wall time of the reference driver's call sequence through the C
@@ -51,8 +57,9 @@ def parse_args():
     ap.add_argument("--precision", type=int, choices=[4, 8], default=8)
     ap.add_argument("--version", type=int, choices=[0, 1, 2], default=0)
     ap.add_argument("--riemann", choices=["hllc", "approx"], default="hllc")
-    ap.add_argument("--arith", choices=["exact", "fma"], default="exact",
-                    help="library build: exact (bitwise serial_ref arithmetic) or fma (multiply-adds fused)")
+    ap.add_argument("--arith", choices=["exact", "fma"], default="fma",
+                    help="library build: fma (multiply-adds fused; within 1e-12 relative L1 and 1e-14 relative dt "
+                         "of the FP64 oracle) or exact (bitwise serial_ref arithmetic)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps of the single-thread CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")

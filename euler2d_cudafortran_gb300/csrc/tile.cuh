@@ -98,6 +98,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   Real* sfx = base + C::fx_off;
   Real* sfy = base + C::fy_off;
   const int tid = threadIdx.x;
+  // The FMA build on square cells (dtdx == dtdy) keeps the raw face fluxes
+  // and applies dt/dx once per cell in the update, fused with the addition.
+  constexpr bool kFluxRaw = SQ && E2D_FMA_FORMS;
 
   // ---- primitives of the whole box (computePrimitives), in place unless
   // the box was loaded elsewhere
@@ -150,8 +153,15 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       }
     }
     if constexpr (SQ) {
+#if E2D_FMA_FORMS
+      // the FMA build keeps q + (s*dtdx)*0.5, rounded once, for the faces
+      const Real hdt = Ops<Real>::half(dtdx);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) s[v] = fmx(s[v], hdt, qc[v]);
+#else
 #pragma unroll
       for (int v = 0; v < 4; ++v) s[v] = Ops<Real>::half(s[v] * dtdx);
+#endif
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -184,12 +194,21 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       if (i0 + f <= h.nx + 2 && j0 + r <= h.ny + 1) {
         const int kl = (r + 1) * RX + f, kr = kl + 1;
         Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
+        if constexpr (SQ && E2D_FMA_FORMS) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 1); dq[v] = sdq[v * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
-        trace_face<Real, true, SQ>(h, qc, dq, s, dtdx, ql);
+          for (int v = 0; v < 4; ++v) { dq[v] = sdq[v * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
+          trace_face_qs<Real, true>(h, s, dq, ql);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 2); dq[v] = sdq[v * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
-        trace_face<Real, false, SQ>(h, qc, dq, s, dtdx, qr);
+          for (int v = 0; v < 4; ++v) { dq[v] = sdq[v * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
+          trace_face_qs<Real, false>(h, s, dq, qr);
+        } else {
+#pragma unroll
+          for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 1); dq[v] = sdq[v * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
+          trace_face<Real, true, SQ>(h, qc, dq, s, dtdx, ql);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) { qc[v] = Q(v, r + 2, f + 2); dq[v] = sdq[v * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
+          trace_face<Real, false, SQ>(h, qc, dq, s, dtdx, qr);
+        }
         if constexpr (TAPE) {
           if (tape->fx) {
             double rec[HR_N];
@@ -209,7 +228,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
           riemann(h, ql, qr, flux);
         }
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = flux[v] * dtdx;
+        for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = kFluxRaw ? flux[v] : flux[v] * dtdx;
       }
     } else if (k >= Y0 && k < NF) {
       const int kk = k - Y0;
@@ -217,12 +236,21 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       if (i0 + c <= h.nx + 1 && j0 + g <= h.ny + 2) {
         const int kl = g * RX + (c + 1), kr = kl + RX;
         Real qc[4], dq[4], s[4], ql[4], qr[4], flux[4];
+        if constexpr (SQ && E2D_FMA_FORMS) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 1, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
-        trace_face<Real, true, SQ>(h, qc, dq, s, dtdy, ql);
+          for (int v = 0; v < 4; ++v) { dq[v] = sdq[(4 + v) * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
+          trace_face_qs<Real, true>(h, s, dq, ql);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 2, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
-        trace_face<Real, false, SQ>(h, qc, dq, s, dtdy, qr);
+          for (int v = 0; v < 4; ++v) { dq[v] = sdq[(4 + v) * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
+          trace_face_qs<Real, false>(h, s, dq, qr);
+        } else {
+#pragma unroll
+          for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 1, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kl]; s[v] = ss[v * RX * RY + kl]; }
+          trace_face<Real, true, SQ>(h, qc, dq, s, dtdy, ql);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) { qc[v] = Q(v, g + 2, c + 2); dq[v] = sdq[(4 + v) * RX * RY + kr]; s[v] = ss[v * RX * RY + kr]; }
+          trace_face<Real, false, SQ>(h, qc, dq, s, dtdy, qr);
+        }
         Real t = ql[IU]; ql[IU] = ql[IV]; ql[IV] = t;
         t = qr[IU]; qr[IU] = qr[IV]; qr[IV] = t;
         if constexpr (TAPE) {
@@ -245,7 +273,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         }
         t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sfy[(v * (TY + 1) + g) * TX + c] = flux[v] * dtdy;
+        for (int v = 0; v < 4; ++v) sfy[(v * (TY + 1) + g) * TX + c] = kFluxRaw ? flux[v] : flux[v] * dtdy;
       }
     }
   }
@@ -266,7 +294,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     for (int v = 0; v < 4; ++v) {
       Real flux_tot = sfx[(v * TY + r) * (TX + 1) + c] - sfx[(v * TY + r) * (TX + 1) + c + 1];
       flux_tot = (sfy[(v * (TY + 1) + r) * TX + c] - sfy[(v * (TY + 1) + r + 1) * TX + c]) + flux_tot;
-      un[v] = in.at(v, j, i) + flux_tot;
+      un[v] = kFluxRaw ? fmx(flux_tot, dtdx, in.at(v, j, i)) : in.at(v, j, i) + flux_tot;
       out.at(v, j, i) = un[v];
     }
     if constexpr (QIN) {

@@ -8,11 +8,22 @@ Two checks of dJ/d(initial density), J = sum rho^2 w (Gaussian w of width
   directional derivatives must agree to round-off, with dt frozen and with dt
   differentiated through the running CFL maximum;
 * against central finite differences of the GPU forward run (eps = 1e-6)
-  with dt frozen.  The implode state is exactly flat on both sides of its
+  with dt frozen, to 1e-6 relative.  The implode state is exactly flat on both sides of its
   interface, where the MC limiter (dlft*drgt = 0) and the CFL maximum (every
   flat cell ties) are not differentiable, so the finite-difference check uses
   the implode state with a 1% smooth modulation of its density and smooth
   random directions, where J is differentiable.
+
+Both library builds are checked: the exact one and the one with fused
+multiply-adds (`arith`), whose forward values differ from the oracle's by
+rounding only.  Where the exact arithmetic has exact ties -- the implode
+state's flat cells all share the CFL maximum, and its x <-> y symmetry makes
+limiter candidates equal -- the FMA rounding breaks them differently, so its
+one-sided derivative there is not the oracle tangent's (the dt adjoint goes
+to another of the tied cells: 2e-5 relative at 64^2 x 30 steps).  The FMA
+build is therefore checked against the tangent on the modulated state,
+where J is differentiable, to 1e-7 relative, and against finite differences
+like the exact build.
 """
 import os
 
@@ -22,6 +33,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 NTHREADS = os.cpu_count() or 1
+FD_TOL = 1e-6  # specification: the adjoint gradient matches finite differences to 1e-6 relative
+TANGENT_TOL = {"exact": 1e-9, "fma": 1e-7}  # against the oracle's forward-mode tangent
+
+
+@pytest.fixture(params=["exact", "fma"])
+def arith(request):
+    return request.param
 
 
 def smooth_base(O, p, amp=1e-2):
@@ -52,27 +70,30 @@ def params(E, O, n):
 
 @pytest.mark.parametrize("base", ["implode", "smooth"])
 @pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
-def test_adjoint_matches_forward_mode_tangent(e2d, oracle, base, dt_mode):
+def test_adjoint_matches_forward_mode_tangent(e2d, oracle, base, dt_mode, arith):
+    if arith == "fma" and base == "implode":
+        pytest.skip("the implode state ties exactly in the exact arithmetic; FMA rounding breaks the ties "
+                    "differently (see the module docstring)")
     n, steps = 64, 30
     pe, po = params(e2d, oracle, n)
     u0 = oracle.init_implode(po) if base == "implode" else smooth_base(oracle, po)
     rng = np.random.default_rng(11 + dt_mode)
-    with e2d.Adjoint(pe) as A:
+    with e2d.Adjoint(pe, arith=arith) as A:
         J, g, dts = A.gradient(steps, u0, dt_mode=dt_mode)
     for _ in range(3):
         d = rng.normal(size=(n, n))
         Jt, dJt = oracle.tangent(po, u0, d, steps, nthreads=NTHREADS, fixed_dts=dts if dt_mode == 0 else None)
         assert abs(J - Jt) <= 1e-13 * abs(Jt)
         dJa = float(np.sum(g * d))
-        assert abs(dJa - dJt) <= 1e-9 * abs(dJt), (dJa, dJt)
+        assert abs(dJa - dJt) <= TANGENT_TOL[arith] * abs(dJt), (dJa, dJt)
 
 
-def test_adjoint_matches_finite_differences(e2d, oracle):
+def test_adjoint_matches_finite_differences(e2d, oracle, arith):
     n, steps, eps = 64, 30, 1e-6
     pe, po = params(e2d, oracle, n)
     u0 = smooth_base(oracle, po)
     rng = np.random.default_rng(7)
-    with e2d.Adjoint(pe) as A:
+    with e2d.Adjoint(pe, arith=arith) as A:
         J, g, dts = A.gradient(steps, u0, dt_mode=0)
         errs = []
         for _ in range(4):
@@ -82,21 +103,23 @@ def test_adjoint_matches_finite_differences(e2d, oracle):
             um[0, 2:-2, 2:-2] -= eps * d
             fd = (A.objective(steps, up, dt_fixed=dts) - A.objective(steps, um, dt_fixed=dts)) / (2 * eps)
             errs.append(abs(fd - np.sum(g * d)) / abs(fd))
-    assert max(errs) < 1e-5, errs
+    print(f"adjoint 64^2 x 30 ({arith}): FD max rel err {max(errs):.2e}")
+    assert max(errs) < FD_TOL, errs
 
 
-def test_adjoint_512_200_steps(e2d, oracle):
+def test_adjoint_512_200_steps(e2d, oracle, arith):
     """The adjoint case: 512^2, 200 steps, HLLC; tangent agreement on the
     implode state and finite differences (16 smooth directions) on the
     modulated state; the adjoint costs at most a few forward runs."""
     n, steps, eps = 512, 200, 1e-6
     pe, po = params(e2d, oracle, n)
-    with e2d.Adjoint(pe) as A:
-        u0 = oracle.init_implode(po)
+    with e2d.Adjoint(pe, arith=arith) as A:
+        # the implode state for the exact build, the modulated one for the FMA build
+        u0 = oracle.init_implode(po) if arith == "exact" else smooth_base(oracle, po)
         J, g, dts = A.gradient(steps, u0, dt_mode=1)
         d = np.random.default_rng(1).normal(size=(n, n))
         Jt, dJt = oracle.tangent(po, u0, d, steps, nthreads=NTHREADS)
-        assert abs(float(np.sum(g * d)) - dJt) <= 1e-9 * abs(dJt)
+        assert abs(float(np.sum(g * d)) - dJt) <= TANGENT_TOL[arith] * abs(dJt)
         us = smooth_base(oracle, po)
         J, g, dts = A.gradient(steps, us, dt_mode=0)
         grad_ms = A.last_ms()[1]
@@ -111,8 +134,9 @@ def test_adjoint_512_200_steps(e2d, oracle):
             um[0, 2:-2, 2:-2] -= eps * dd
             fd = (A.objective(steps, up, dt_fixed=dts) - A.objective(steps, um, dt_fixed=dts)) / (2 * eps)
             errs.append(abs(fd - np.sum(g * dd)) / abs(fd))
-    print(f"adjoint 512^2 x 200: FD max rel err {max(errs):.2e}, gradient/forward time {grad_ms / fwd_ms:.2f}")
-    assert max(errs) < 1e-4, errs
+    print(f"adjoint 512^2 x 200 ({arith}): FD max rel err {max(errs):.2e}, "
+          f"gradient/forward time {grad_ms / fwd_ms:.2f}")
+    assert max(errs) < FD_TOL, errs
 
 
 @pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
@@ -139,7 +163,7 @@ def test_tape_gives_the_recomputed_gradient(e2d, oracle, monkeypatch, dt_mode):
 
 
 @pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
-def test_whole_tape_gives_the_segmented_gradient(e2d, oracle, monkeypatch, dt_mode):
+def test_whole_tape_gives_the_segmented_gradient(e2d, oracle, monkeypatch, dt_mode, arith):
     """When every state and its tape fit in memory the forward sweep keeps
     them all and nothing is recomputed; with E2D_ADJ_FULL_TAPE=0 the run is
     checkpointed in segments whose states and tapes are recomputed during the
@@ -150,11 +174,11 @@ def test_whole_tape_gives_the_segmented_gradient(e2d, oracle, monkeypatch, dt_mo
     po = oracle.Params(nx=72, ny=88, gamma0=1.4, cfl=0.8, riemann=2, bc_xmin=2, bc_ymin=3, bc_ymax=3)
     u0 = smooth_base(oracle, po)
     n = 29  # K = 6 when segmented: a ragged last segment
-    with e2d.Adjoint(p) as a:
+    with e2d.Adjoint(p, arith=arith) as a:
         J1, g1, d1 = a.gradient(n, u0, dt_mode=dt_mode)
         assert a.layout() == (n, True)
     monkeypatch.setenv("E2D_ADJ_FULL_TAPE", "0")
-    with e2d.Adjoint(p) as b:
+    with e2d.Adjoint(p, arith=arith) as b:
         J2, g2, d2 = b.gradient(n, u0, dt_mode=dt_mode)
         assert b.layout() == (6, True)
     assert np.array_equal(d1, d2)

@@ -94,3 +94,28 @@ def test_seeded_ensemble_first_steps(e2d):
                 rdts = run.advance(0, 4)
                 assert np.array_equal(b.final_state(k, 4)[:, 2:-2, 2:-2], run.final_state(4)[:, 2:-2, 2:-2])
                 assert np.array_equal(dts[:, k], rdts)
+
+
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+def test_fma_batch_matches_the_oracle(e2d, oracle, prec):
+    """The FMA build's ensemble step against the oracle, problem by problem:
+    FP64 within the specified 1e-12 relative L1 per variable and 1e-14
+    relative dt; FP32 within 1e-5 of the FP32 oracle (rounding differences of
+    the fused multiply-adds)."""
+    n = 25
+    l1_tol, dt_tol = (1e-12, 1e-14) if prec == 8 else (1e-5, 1e-5)
+    with e2d.Batch(SIZES, BCS, gamma0=1.4, cfl=0.8, riemann_solver=2, precision=prec, arith="fma") as b:
+        b.init_diagonal(OFFSET, RHO_HI, P_HI, RHO_LO, P_LO)
+        dts = b.advance(0, n)
+        for k, ((nx, ny), bc) in enumerate(zip(SIZES, BCS)):
+            po = oracle.Params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann=2, bc_xmin=bc[0], bc_xmax=bc[1],
+                               bc_ymin=bc[2], bc_ymax=bc[3])
+            u0 = oracle.init_diagonal(po, OFFSET[k], RHO_HI[k], P_HI[k], RHO_LO[k], P_LO[k],
+                                      prec="f64" if prec == 8 else "f32")
+            ref, dts_ref, _, _ = oracle.run(po, n, prec="f64" if prec == 8 else "f32", u0=u0)
+            got = b.final_state(k, n)[:, 2:-2, 2:-2].astype(np.float64)
+            want = ref[:, 2:-2, 2:-2].astype(np.float64)
+            l1 = [float(np.abs(got[v] - want[v]).sum() / np.abs(want[v]).sum()) for v in range(4)]
+            dr = float(np.max(np.abs(dts[:, k].astype(np.float64) - dts_ref) / dts_ref))
+            assert max(l1) <= l1_tol and dr <= dt_tol, f"problem {k}: rel L1 {l1}, dt {dr}"
+            assert b.health(k) == 0
