@@ -320,6 +320,25 @@ __device__ __forceinline__ void trace_sources(const Hydro<Real>& h, const Real q
   s[IV] = ((-(u * dqx[IV])) - (v * dqy[IV])) - O::div(dqy[IP], r);
 }
 
+// The FMA build's cell value for its four face states on square cells:
+// qs = q + (s*dtdx)*0.5 with the sources of trace_sources written as
+// s = -(u*dqx + v*dqy + t), t the last term of each source, and
+// qs = q - (dtdx/2)*(u*dqx + v*dqy + t), every step a fused multiply-add.
+template <typename Real>
+__device__ __forceinline__ void trace_qs(const Hydro<Real>& h, const Real q[4], const Real dqx[4], const Real dqy[4],
+                                         Real hdt, Real qs[4]) {
+  using O = Ops<Real>;
+  const Real r = q[ID], p = q[IP], u = q[IU], v = q[IV];
+  const Real dv = dqx[IU] + dqy[IV];
+  Real t[4];
+  t[ID] = dv * r;
+  t[IP] = (dv * h.gamma0) * p;
+  t[IU] = O::div(dqx[IP], r);
+  t[IV] = O::div(dqy[IP], r);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qs[k] = fmx(-hdt, fmx(u, dqx[k], fmx(v, dqy[k], t[k])), q[k]);
+}
+
 // Face state of trace_unsplit_2d_along_dir, serial_ref/m_utils.f90:218-252:
 // qf = (q -/+ 0.5*dq_dir) + (s*dtd)*0.5, then rho floored at smallr.
 // PLUS selects the XMAX/YMAX faces; dq is the slope along the face normal,

@@ -140,7 +140,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       qn[v] = Q(v, y + 1, x); qs[v] = Q(v, y - 1, x);
     }
     slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
+#if E2D_FMA_FORMS
+    // the FMA build on square cells forms q + (s*dtdx)*0.5 directly
+    if constexpr (SQ && !TAPE) trace_qs(h, qc, dqx, dqy, Ops<Real>::half(dtdx), s);
+    else trace_sources(h, qc, dqx, dqy, s);
+#else
     trace_sources(h, qc, dqx, dqy, s);
+#endif
     if constexpr (TAPE) {
       const int gi = i0 - GW + x, gj = j0 - GW + y;
       if (gi <= h.nx + 2 && gj <= h.ny + 2 && owns(gi, i0, TX, h.nx) && owns(gj, j0, TY, h.ny)) {
@@ -154,10 +160,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     }
     if constexpr (SQ) {
 #if E2D_FMA_FORMS
-      // the FMA build keeps q + (s*dtdx)*0.5, rounded once, for the faces
-      const Real hdt = Ops<Real>::half(dtdx);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) s[v] = fmx(s[v], hdt, qc[v]);
+      // the FMA build keeps q + (s*dtdx)*0.5 for the faces (formed above
+      // unless the tape needed s itself)
+      if constexpr (TAPE) trace_qs(h, qc, dqx, dqy, Ops<Real>::half(dtdx), s);  // as the step without a tape
 #else
 #pragma unroll
       for (int v = 0; v < 4; ++v) s[v] = Ops<Real>::half(s[v] * dtdx);
