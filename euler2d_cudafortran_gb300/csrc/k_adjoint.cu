@@ -373,6 +373,261 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
   }
 }
 
+// ---- the reverse step of square cells reading a tape, in less shared memory
+//
+// With a tape and dx == dy the face pass needs neither the slopes nor the
+// sources of its cells: the face states (and whether the density floor
+// acted on them) are in the face's recorded solve, and the dt adjoint of the
+// face source terms, sum over a cell's face states of s * (face adjoint)/2,
+// is s times the cell's summed source adjoint, which the ring pass forms
+// from the tape's s.  The ring pass reads the slopes and sources from the
+// tape in global memory.  Shared memory then holds the primitives box, the
+// next adjoint, the ring and box adjoints and one scratch plane set: 73 KB,
+// so three CTAs of 128 threads fit on an SM instead of two.
+#ifndef E2D_REVT_MINB
+#define E2D_REVT_MINB 3
+#endif
+constexpr int T_Q_OFF = 0;                    // q box      [4][ABY][ABX] (the tape's primitives)
+constexpr int T_UB_OFF = T_Q_OFF + 4 * NBOX;  // Ubar'      [4][ATY+1][ATX+1]
+constexpr int T_RA_OFF = T_UB_OFF + 4 * NUB;  // ring adj.  dqx[4] dqy[4] s[4]: [12][ARY][ARX]
+constexpr int T_QB_OFF = T_RA_OFF + 12 * NRING;  // q adjoint  [4][ABY][ABX]
+constexpr int T_SC_OFF = T_QB_OFF + 4 * NBOX;  // scratch    [4][ARY][ARX] (south limiter adjoints)
+constexpr int T_N_SMEM = T_SC_OFF + 4 * NRING;
+constexpr size_t T_SMEM_BYTES = (size_t)T_N_SMEM * sizeof(double) + 64;
+
+__device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<double> un, Field<double> ubn1,
+                                                  Field<double> ubn, Field<double> ubz, double dt, double* dtbar,
+                                                  int bx, int by, double* sm, const TapeOut& tape) {
+  double* sq = sm + T_Q_OFF;
+  double* sub = sm + T_UB_OFF;
+  double* sra = sm + T_RA_OFF;
+  double* sqb = sm + T_QB_OFF;
+  double* ssc = sm + T_SC_OFF;
+  __shared__ double red[ANT / 32];
+  const int tid = threadIdx.x;
+  const int i0 = GW + bx * ATX, j0 = GW + by * ATY;
+  const double dtdx = Ops<double>::div(dt, h.dx);  // == dt / dy
+  if (ubz.p) {
+    for (int k = tid; k < 4 * ATX * ATY; k += ANT) {
+      const int v = k / (ATX * ATY), rem = k - v * (ATX * ATY), y = rem / ATX, x = rem - y * ATX;
+      if (i0 + x <= h.nx + 1 && j0 + y <= h.ny + 1) ubz.at(v, j0 + y, i0 + x) = 0.0;
+    }
+  }
+  for (int k = tid; k < 4 * NBOX; k += ANT) {
+    const int v = k / NBOX, rem = k - v * NBOX, y = rem / ABX, x = rem - y * ABX;
+    const int gi = i0 - GW + x, gj = j0 - GW + y;
+    sq[k] = (gi < h.isize && gj < h.jsize) ? tape.at(tape.q, v, gj, gi) : 0.0;
+    sqb[k] = 0.0;
+  }
+  for (int k = tid; k < 12 * NRING; k += ANT) sra[k] = 0.0;
+  for (int k = tid; k < 4 * NUB; k += ANT) {
+    const int v = k / NUB, rem = k - v * NUB, y = rem / (ATX + 1), x = rem - y * (ATX + 1);
+    const int gi = i0 - 1 + x, gj = j0 - 1 + y;
+    const bool interior = gi >= GW && gi <= h.nx + 1 && gj >= GW && gj <= h.ny + 1;
+    sub[k] = interior ? ubn1.at(v, gj, gi) : 0.0;
+  }
+  __syncthreads();
+  auto Q = [&](int v, int y, int x) -> double { return sq[(v * ABY + y) * ABX + x]; };
+  auto UB = [&](int v, int i, int j) -> double {  // Ubar' of absolute cell (i, j), zero outside the interior
+    const int x = i - (i0 - 1), y = j - (j0 - 1);
+    return (x >= 0 && x <= ATX && y >= 0 && y <= ATY) ? sub[(v * (ATY + 1) + y) * (ATX + 1) + x] : 0.0;
+  };
+
+  // ---- owned faces (four conflict-free passes, as in step_rev_tile):
+  // flux adjoint -> recorded Riemann solve reverse -> face-state adjoints
+  // added to the cell, its normal slope and its (per unit dtdx) sources
+  double dtb = 0.0;  // dt/dx adjoint of the fluxes
+  constexpr int NFX_EVEN = ATX / 2 + 1, NFX_ODD = (ATX + 1) / 2;
+  constexpr int NGY_EVEN = ATY / 2 + 1, NGY_ODD = (ATY + 1) / 2;
+  static_assert(NFX_EVEN * ATY <= ANT && NGY_EVEN * ATX <= ANT, "one face per thread per pass");
+#pragma unroll 1
+  for (int pass = 0; pass < 4; ++pass) {
+    const bool xface = pass < 2;
+    const int par = pass & 1;
+    const int nfx = par ? NFX_ODD : NFX_EVEN;
+    const int nf = xface ? nfx * ATY : (par ? NGY_ODD : NGY_EVEN) * ATX;
+    int a = 0, b = 0, ka = 0, kb = 0, fi = 0, fj = 0;
+    double fb[4];
+    bool valid = tid < nf;
+    if (xface) {
+      const int f = 2 * (tid % nfx) + par, r = tid / nfx;
+      fi = i0 + f; fj = j0 + r;
+      valid = valid && fi <= h.nx + 2 && fj <= h.ny + 1 && (f < ATX || fi == h.nx + 2);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fb[v] = valid ? UB(v, fi, fj) - UB(v, fi - 1, fj) : 0.0;
+      a = (r + 1) * ARX + f;
+      b = a + 1;
+      ka = (r + 2) * ABX + (f + 1);
+      kb = ka + 1;
+    } else {
+      const int c = tid % ATX, g = 2 * (tid / ATX) + par;
+      fi = i0 + c; fj = j0 + g;
+      valid = valid && fi <= h.nx + 1 && fj <= h.ny + 2 && (g < ATY || fj == h.ny + 2);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fb[v] = valid ? UB(v, fi, fj) - UB(v, fi, fj - 1) : 0.0;
+      a = g * ARX + (c + 1);
+      b = a + ARX;
+      ka = (g + 1) * ABX + (c + 2);
+      kb = ka + ABX;
+    }
+    if (valid) {
+      double rb[4];
+      if (xface) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) rb[v] = fb[v] * dtdx;
+      } else {  // the stored y flux is the Riemann flux with IU and IV swapped back
+        rb[ID] = fb[ID] * dtdx; rb[IP] = fb[IP] * dtdx; rb[IU] = fb[IV] * dtdx; rb[IV] = fb[IU] * dtdx;
+      }
+      double rec[HR_N];
+      double* fr = xface ? tape.fx : tape.fy;
+#pragma unroll
+      for (int e = 0; e < HR_N; ++e) rec[e] = tape.at(fr, e, fj, fi);
+      const unsigned fl = tape.flag(xface ? tape.flx : tape.fly, fj, fi);
+      double qlb[4] = {0, 0, 0, 0}, qrb[4] = {0, 0, 0, 0};
+      adj::riemann_hllc_rev_rec(h, rec, fl, rb, qlb, qrb);
+      if (xface) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) dtb += rec[HR_FLUX + v] * fb[v];
+      } else {
+        dtb += rec[HR_FLUX + ID] * fb[ID] + rec[HR_FLUX + IP] * fb[IP] + rec[HR_FLUX + IV] * fb[IU] +
+               rec[HR_FLUX + IU] * fb[IV];
+        double t = qlb[IU]; qlb[IU] = qlb[IV]; qlb[IV] = t;
+        t = qrb[IU]; qrb[IU] = qrb[IV]; qrb[IV] = t;
+      }
+      // density floor max(smallr, raw) of each face state, from the
+      // recorded state: no gradient where it returned smallr
+      if (!emul::gt_i(rec[HR_QL + ID], h.smallr)) qlb[ID] = 0.0;
+      if (!emul::gt_i(rec[HR_QR + ID], h.smallr)) qrb[ID] = 0.0;
+      const int nrm = xface ? 0 : 4;  // slope block of the face normal
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double hl = Ops<double>::half(qlb[v]), hr = Ops<double>::half(qrb[v]);
+        sqb[v * NBOX + ka] += qlb[v];         // cell a's plus face (XMAX / YMAX)
+        sqb[v * NBOX + kb] += qrb[v];         // cell b's minus face
+        sra[(nrm + v) * NRING + a] += hl;
+        sra[(nrm + v) * NRING + b] -= hr;
+        sra[(8 + v) * NRING + a] += hl;
+        sra[(8 + v) * NRING + b] += hr;
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- ring cells: the dt adjoint of their face source terms, then
+  // sources and slopes reverse (limiter neighbours' adjoints left in the
+  // cell's own slots for the box pass, as in step_rev_tile)
+  const bool mc = h.slope_type == 2;
+  const bool lim = h.slope_type == 1 || h.slope_type == 2;
+  double dts = 0.0;  // dt/dx adjoint of the source terms
+  for (int k = tid; k < NRING; k += ANT) {
+    const int x = k % ARX + 1, y = k / ARX + 1;
+    const int gi = i0 - GW + x, gj = j0 - GW + y;
+    const bool in = gi <= h.nx + 2 && gj <= h.ny + 2;
+    double qc[4], dqx[4], dqy[4], sbar[4], dqxb[4], dqyb[4], qcb[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qc[v] = Q(v, y, x);
+      dqx[v] = in ? tape.at(tape.dq, v, gj, gi) : 0.0;
+      dqy[v] = in ? tape.at(tape.dq, 4 + v, gj, gi) : 0.0;
+      const double sv = in ? tape.at(tape.s, v, gj, gi) : 0.0;
+      dqxb[v] = sra[v * NRING + k]; dqyb[v] = sra[(4 + v) * NRING + k];
+      const double sb = sra[(8 + v) * NRING + k];  // summed per unit dtdx by the face pass
+      dts += sv * sb;
+      sbar[v] = sb * dtdx;
+    }
+    adj::trace_sources_rev(h, qc, dqx, dqy, sbar, qcb, dqxb, dqyb);
+    const int kc = y * ABX + x;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double qe = 0, qw = 0, qn = 0, qs = 0;
+      if (lim) {
+        adj::slope1_rev(mc, qc[v], Q(v, y, x + 1), Q(v, y, x - 1), dqxb[v], qcb[v], qe, qw);
+        adj::slope1_rev(mc, qc[v], Q(v, y + 1, x), Q(v, y - 1, x), dqyb[v], qcb[v], qn, qs);
+      }
+      sqb[v * NBOX + kc] += qcb[v];
+      sra[v * NRING + k] = qe;
+      sra[(4 + v) * NRING + k] = qw;
+      sra[(8 + v) * NRING + k] = qn;
+      ssc[v * NRING + k] = qs;
+    }
+  }
+  __syncthreads();
+
+  // ---- box cells: gather, primitives reverse, ghost folding, update identity
+  auto ring_of = [&](int x, int y) -> int {
+    return (x >= 1 && x <= ARX && y >= 1 && y <= ARY) ? (y - 1) * ARX + (x - 1) : -1;
+  };
+  for (int k = tid; k < NBOX; k += ANT) {
+    const int y = k / ABX, x = k - y * ABX;
+    const int gi = i0 - GW + x, gj = j0 - GW + y;
+    if (gi >= h.isize || gj >= h.jsize) continue;
+    const bool xin = gi >= GW && gi <= h.nx + 1, yin = gj >= GW && gj <= h.ny + 1;
+    if (!xin && !yin) continue;  // corner: a constant
+    double qb[4], u[4], ub[4] = {0, 0, 0, 0};
+    const int rw = ring_of(x - 1, y), re = ring_of(x + 1, y), rs = ring_of(x, y - 1), rn = ring_of(x, y + 1);
+    bool any = false;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double t = sqb[v * NBOX + k];
+      if (rw >= 0) t += sra[v * NRING + rw];
+      if (re >= 0) t += sra[(4 + v) * NRING + re];
+      if (rs >= 0) t += sra[(8 + v) * NRING + rs];
+      if (rn >= 0) t += ssc[v * NRING + rn];
+      qb[v] = t;
+      any |= (emul::bits(t) << 1) != 0;
+    }
+    if (any) {
+      double qf[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { u[v] = un.at(v, gj, gi); qf[v] = sq[v * NBOX + k]; }
+      adj::primitives_rev_q(h, u, qf, qb, ub);
+    }
+    if (xin && yin) {
+      if (gi >= i0 && gi < i0 + ATX && gj >= j0 && gj < j0 + ATY) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) ub[v] += UB(v, gi, gj);
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+        if ((emul::bits(ub[v]) << 1) != 0) atomicAdd(&ubn.at(v, gj, gi), ub[v]);
+    } else if (any) {
+      int si = gi, sj = gj, type, flip;
+      if (!xin) {
+        type = gi < GW ? h.bc_xmin : h.bc_xmax;
+        si = ghost_source(gi, h.nx, type);
+        flip = IU;
+      } else {
+        type = gj < GW ? h.bc_ymin : h.bc_ymax;
+        sj = ghost_source(gj, h.ny, type);
+        flip = IV;
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double g = Ops<double>::neg_if(ub[v], type == 1 && v == flip);
+        if ((emul::bits(g) << 1) != 0) atomicAdd(&ubn.at(v, sj, si), g);
+      }
+    }
+  }
+  // ---- dt adjoint: dtdx = dt/dx (== dt/dy)
+  double d = dtb + dts;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if ((tid & 31) == 0) red[tid >> 5] = d;
+  __syncthreads();
+  if (tid == 0) {
+    double sx = 0;
+    for (int w = 0; w < ANT / 32; ++w) sx += red[w];
+    atomicAdd(dtbar, sx / h.dx);
+  }
+}
+
+__global__ void __launch_bounds__(ANT, E2D_REVT_MINB)
+    k_step_rev_tsq(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, Field<double> ubz,
+                   const double* dt, double* dtbar, TapeOut tape) {
+  extern __shared__ double sm[];
+  step_rev_tile_tsq(h, un, ubn1, ubn, ubz, *dt, dtbar, blockIdx.x, blockIdx.y, sm, tape);
+}
+
 template <bool SQ, bool TAPE>
 __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
     k_step_rev(Hydro<double> h, Field<double> un, Field<double> ubn1, Field<double> ubn, Field<double> ubz,
@@ -597,6 +852,33 @@ __global__ void __launch_bounds__(ANT, E2D_REV_MINB)
                           dtbar_log + row, tile % P.ntx, tile / P.ntx, sm, tp);
 }
 
+// The batched reverse step of square cells reading the tape (see step_rev_tile_tsq).
+__global__ void __launch_bounds__(ANT, E2D_REVT_MINB)
+    k_batch_step_rev_tsq(const AdjProb* __restrict__ probs, int nprob, const double* dt_log, double* dtbar_log,
+                         int un, int ub_in, int ub_out, int ub_zero, int m, int tape_j) {
+  extern __shared__ double sm[];
+  __shared__ Hydro<double> sh;
+  __shared__ int sp;
+  const int t = blockIdx.x;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nprob - 1;  // last problem with tile_begin <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].tile_begin <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    sp = lo;
+    sh = probs[lo].h;
+  }
+  __syncthreads();
+  const AdjProb& P = probs[sp];
+  const int tile = t - P.tile_begin;
+  const long long row = (long long)m * nprob + sp;
+  step_rev_tile_tsq(sh, afield(P, un), afield(P, ub_in), afield(P, ub_out),
+                    ub_zero >= 0 ? afield(P, ub_zero) : Field<double>{nullptr, 0, 0}, dt_log[row], dtbar_log + row,
+                    tile % P.ntx, tile / P.ntx, sm, tape_at(P.tape_base, tape_j, P.plane, P.pitch, false));
+}
+
 __global__ void k_batch_argmax(const AdjProb* __restrict__ probs, int nprob, const double* inv_log, int un, int m,
                                double* pv, long long* pi) {
   const int p = blockIdx.y;
@@ -662,6 +944,8 @@ int step_rev_setup() {
   bool ok = true;
   for (auto f : {k_step_rev<false, false>, k_step_rev<true, false>, k_step_rev<false, true>, k_step_rev<true, true>})
     ok = ok && cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) == cudaSuccess;
+  ok = ok && cudaFuncSetAttribute(k_step_rev_tsq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T_SMEM_BYTES) ==
+                 cudaSuccess;
   return ok ? 0 : -1;
 }
 
@@ -671,7 +955,7 @@ void launch_step_rev(const Hydro<double>& h, Field<double> un, Field<double> ubn
   const TapeOut t = tape ? *tape : TapeOut();
   const bool sq = h.dx == h.dy;
   if (tape) {
-    if (sq) k_step_rev<true, true><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
+    if (sq) k_step_rev_tsq<<<g, ANT, T_SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
     else k_step_rev<false, true><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
   } else {
     if (sq) k_step_rev<true, false><<<g, ANT, SMEM_BYTES, s>>>(h, un, ubn1, ubn, ubz, dt, dtbar, t);
@@ -707,6 +991,8 @@ int batch_step_rev_setup() {
   for (auto f : {k_batch_step_rev<false, false>, k_batch_step_rev<true, false>, k_batch_step_rev<false, true>,
                  k_batch_step_rev<true, true>})
     ok = ok && cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) == cudaSuccess;
+  ok = ok && cudaFuncSetAttribute(k_batch_step_rev_tsq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)T_SMEM_BYTES) == cudaSuccess;
   return ok ? 0 : -1;
 }
 
@@ -723,7 +1009,9 @@ void launch_batch_step_rev(const AdjBatch& B, int un, int ub_in, int ub_out, int
                                                 m, tape_j);
   };
   if (tape_j >= 0) {
-    if (B.square) args(k_batch_step_rev<true, true>);
+    if (B.square)
+      k_batch_step_rev_tsq<<<B.total_tiles, ANT, T_SMEM_BYTES, s>>>(B.probs, B.nprob, B.dt_log, B.dtbar_log, un, ub_in,
+                                                                   ub_out, ub_zero, m, tape_j);
     else args(k_batch_step_rev<false, true>);
   } else {
     if (B.square) args(k_batch_step_rev<true, false>);
