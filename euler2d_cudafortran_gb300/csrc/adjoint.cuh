@@ -103,6 +103,24 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
   }
 }
 
+// The same from the forward step's recorded limiter case (3 bits, LIM_*):
+// nothing of the slope is recomputed.
+__device__ __forceinline__ void slope1_rev_case(bool mc, unsigned cs, double sb, double& qbar, double& qpbar,
+                                                double& qmbar) {
+  const unsigned sel = cs & 3u;
+  if (sel == LIM_ZERO) return;
+  if (sel == LIM_CENTRE) {  // slope = dcen = (qp - qm) / 2
+    const double g = O::half(sb);
+    qpbar += g;
+    qmbar -= g;
+    return;
+  }
+  const double g = O::neg_if(sb, (cs & LIM_FLIP) != 0u);  // dsgn * sign(x) * sb
+  const double sg = mc ? O::twice(g) : g;                 // st * g
+  if (sel == LIM_LEFT) { qbar += sg; qmbar -= sg; }
+  else { qpbar += sg; qbar -= sg; }
+}
+
 // trace_sources reverse: sb -> (qb, dqxb, dqyb).
 __device__ __forceinline__ void trace_sources_rev(const Hydro<double>& h, const double q[4], const double dqx[4],
                                                   const double dqy[4], const double sb[4], double qb[4],

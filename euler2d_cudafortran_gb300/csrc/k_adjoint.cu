@@ -381,9 +381,11 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
 // face source terms, sum over a cell's face states of s * (face adjoint)/2,
 // is s times the cell's summed source adjoint, which the ring pass forms
 // from the tape's s.  The ring pass reads the slopes and sources from the
-// tape in global memory.  Shared memory then holds the primitives box, the
-// next adjoint, the ring and box adjoints and one scratch plane set: 73 KB,
-// so three CTAs of 128 threads fit on an SM instead of two.
+// tape in global memory, and the slopes' reverse takes the limiter cases the
+// forward step recorded (nothing of the slopes is recomputed).  Shared memory
+// then holds the primitives box, the next adjoint, the ring and box adjoints
+// and one scratch plane set: 73 KB, so three CTAs of 128 threads fit on an
+// SM instead of two.
 #ifndef E2D_REVT_MINB
 #define E2D_REVT_MINB 3
 #endif
@@ -537,13 +539,12 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
     }
     adj::trace_sources_rev(h, qc, dqx, dqy, sbar, qcb, dqxb, dqyb);
     const int kc = y * ABX + x;
+    const unsigned cases = (in && lim) ? tape.flag(tape.lim, gj, gi) : 0u;  // the forward's limiter cases
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       double qe = 0, qw = 0, qn = 0, qs = 0;
-      if (lim) {
-        adj::slope1_rev(mc, qc[v], Q(v, y, x + 1), Q(v, y, x - 1), dqxb[v], qcb[v], qe, qw);
-        adj::slope1_rev(mc, qc[v], Q(v, y + 1, x), Q(v, y - 1, x), dqyb[v], qcb[v], qn, qs);
-      }
+      adj::slope1_rev_case(mc, cases >> (3 * v), dqxb[v], qcb[v], qe, qw);
+      adj::slope1_rev_case(mc, cases >> (12 + 3 * v), dqyb[v], qcb[v], qn, qs);
       sqb[v * NBOX + kc] += qcb[v];
       sra[v * NRING + k] = qe;
       sra[(4 + v) * NRING + k] = qw;

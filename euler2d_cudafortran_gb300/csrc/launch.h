@@ -96,6 +96,8 @@ struct TapeOut {
   double* fy = nullptr;
   unsigned* flx = nullptr;
   unsigned* fly = nullptr;
+  // the limiter cases of the ring cells' eight slopes (slopes<Real, true>)
+  unsigned* lim = nullptr;
   int pitch = 0;
   long long plane = 0;
   int only = 0;
@@ -107,9 +109,10 @@ struct TapeOut {
   }
 };
 
-// Planes of one tape: q 4, dq 8, s 4, x and y face records HR_N each, and
-// the two planes of 32-bit face flags in one plane of doubles.
-constexpr int kTapePlanes = 4 + 8 + 4 + 2 * HR_N + 1;
+// Planes of one tape: q 4, dq 8, s 4, x and y face records HR_N each, the
+// two planes of 32-bit face flags in one plane of doubles, and the 32-bit
+// limiter cases in one more.
+constexpr int kTapePlanes = 4 + 8 + 4 + 2 * HR_N + 2;
 
 // Tape j of a run of tapes at `base` (kTapePlanes planes each) of a state
 // with `plane` elements per plane and row pitch `pitch`.
@@ -123,6 +126,7 @@ __host__ __device__ inline TapeOut tape_at(double* base, int j, long long plane,
   t.fy = t.fx + HR_N * plane;
   t.flx = reinterpret_cast<unsigned*>(t.fy + HR_N * plane);
   t.fly = t.flx + plane;
+  t.lim = t.fly + plane;
   t.pitch = pitch;
   t.plane = plane;
   t.only = only ? 1 : 0;

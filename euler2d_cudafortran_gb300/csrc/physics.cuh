@@ -259,18 +259,37 @@ __device__ __forceinline__ bool prod_le0(double a, double b, bool& amb) {
 #endif
 }
 
-template <typename Real, bool INT = false>
-__device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm, bool& amb) {
+// Limiter cases recorded for the adjoint (3 bits per slope): bits 0-1 the
+// selection -- 0 limited to zero, 1 |dlft|, 2 |drgt|, 3 |dcen| -- and bit 2
+// set when the selected one-sided difference has the sign opposite to dcen.
+enum { LIM_ZERO = 0, LIM_LEFT = 1, LIM_RIGHT = 2, LIM_CENTRE = 3, LIM_FLIP = 4 };
+
+template <typename Real, bool INT = false, bool CASE = false>
+__device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm, bool& amb, unsigned* cs = nullptr) {
   using O = Ops<Real>;
   const Real dl = q - qm, dr = qp - q;
   const Real dlft = mc ? O::twice(dl) : dl;
   const Real drgt = mc ? O::twice(dr) : dr;
   const Real dcen = O::half(qp - qm);
-  const Real slop = O::min(rabs(dlft), rabs(drgt));
-  Real dlim;
-  if constexpr (INT) dlim = prod_le0(dlft, drgt, amb) ? Real(0.0) : slop;
-  else dlim = limiter_dlim(dlft, drgt, slop);
-  return O::neg_if(O::min(dlim, rabs(dcen)), !O::ge0(dcen));
+  const Real al = rabs(dlft), ar = rabs(drgt);
+  const Real slop = O::min(al, ar);
+  bool zero;
+  if constexpr (INT) zero = prod_le0(dlft, drgt, amb);
+  else zero = Ops<Real>::le0(dlft * drgt);
+  const Real dlim = zero ? Real(0.0) : slop;
+  const Real ac = rabs(dcen);
+  if constexpr (CASE) {
+    // the selections of O::min, which keeps its first argument when it is
+    // strictly smaller (for double: in the integer order of emul::ord)
+    const bool use_l = !O::ge(al, ar);
+    const bool pick_slop = !O::ge(slop, ac);
+    const Real x = use_l ? dlft : drgt;
+    *cs = zero ? (unsigned)LIM_ZERO
+               : pick_slop ? ((use_l ? (unsigned)LIM_LEFT : (unsigned)LIM_RIGHT) |
+                              ((O::ge0(x) != O::ge0(dcen)) ? (unsigned)LIM_FLIP : 0u))
+                           : (unsigned)LIM_CENTRE;
+  }
+  return O::neg_if(O::min(dlim, ac), !O::ge0(dcen));
 }
 
 // slope_unsplit_hydro_2d, serial_ref/m_utils.f90:268-342.  For double the
@@ -279,31 +298,42 @@ __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm, bool& 
 // the products, in a branch of its own -- a fallback product beside each
 // test would be predicated into every path, and a predicated FP64
 // instruction still takes its FP64 pipe slot.
-template <typename Real>
+// CASE: also return the limiter cases of the eight slopes in *cases (3 bits
+// each, LIM_*: dqx[v] at bits 3v, dqy[v] at bits 12 + 3v; 0 when the slopes
+// are not limited, slope_type 0).
+template <typename Real, bool CASE = false>
 __device__ __forceinline__ void slopes(const Hydro<Real>& h, const Real q[4], const Real qpx[4],
                                        const Real qmx[4], const Real qpy[4], const Real qmy[4],
-                                       Real dqx[4], Real dqy[4]) {
+                                       Real dqx[4], Real dqy[4], unsigned* cases = nullptr) {
   if (h.slope_type == 1 || h.slope_type == 2) {
     const bool mc = h.slope_type == 2;
     bool amb = false;
     constexpr bool INT = sizeof(Real) == 8 && E2D_LIM_INT;
+    unsigned c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      dqx[v] = slope1<Real, INT>(mc, q[v], qpx[v], qmx[v], amb);
-      dqy[v] = slope1<Real, INT>(mc, q[v], qpy[v], qmy[v], amb);
+      dqx[v] = slope1<Real, INT, CASE>(mc, q[v], qpx[v], qmx[v], amb, &c[v]);
+      dqy[v] = slope1<Real, INT, CASE>(mc, q[v], qpy[v], qmy[v], amb, &c[4 + v]);
     }
     if constexpr (INT) {
       if (amb) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          dqx[v] = slope1<Real, false>(mc, q[v], qpx[v], qmx[v], amb);
-          dqy[v] = slope1<Real, false>(mc, q[v], qpy[v], qmy[v], amb);
+          dqx[v] = slope1<Real, false, CASE>(mc, q[v], qpx[v], qmx[v], amb, &c[v]);
+          dqy[v] = slope1<Real, false, CASE>(mc, q[v], qpy[v], qmy[v], amb, &c[4 + v]);
         }
       }
+    }
+    if constexpr (CASE) {
+      unsigned w = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) w |= c[k] << (3 * k);
+      *cases = w;
     }
   } else {
 #pragma unroll
     for (int v = 0; v < 4; ++v) { dqx[v] = Real(0.0); dqy[v] = Real(0.0); }
+    if constexpr (CASE) *cases = 0u;
   }
 }
 

@@ -139,7 +139,8 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
       qc[v] = Q(v, y, x); qe[v] = Q(v, y, x + 1); qw[v] = Q(v, y, x - 1);
       qn[v] = Q(v, y + 1, x); qs[v] = Q(v, y - 1, x);
     }
-    slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
+    unsigned lim_cases = 0;
+    slopes<Real, TAPE>(h, qc, qe, qw, qn, qs, dqx, dqy, &lim_cases);
 #if E2D_FMA_FORMS
     // the FMA build on square cells forms q + (s*dtdx)*0.5 directly
     if constexpr (SQ && !TAPE) trace_qs(h, qc, dqx, dqy, Ops<Real>::half(dtdx), s);
@@ -156,6 +157,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
           tape->at(tape->dq, 4 + v, gj, gi) = dqy[v];
           tape->at(tape->s, v, gj, gi) = s[v];
         }
+        tape->flag(tape->lim, gj, gi) = lim_cases;
       }
     }
     if constexpr (SQ) {

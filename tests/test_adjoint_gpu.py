@@ -152,21 +152,24 @@ def test_adjoint_512_200_steps(e2d, oracle, arith):
 
 
 @pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
-def test_tape_gives_the_recomputed_gradient(e2d, oracle, monkeypatch, dt_mode):
+def test_tape_gives_the_recomputed_gradient(e2d, oracle, monkeypatch, dt_mode, arith):
     """The reverse step reading the forward sweeps' tape (primitives, slopes,
-    sources, recorded HLLC solves) gives the gradient of the reverse step that
-    recomputes them: the same values enter the same reverse arithmetic, so
-    only the order of atomic additions (J, ghost folding, dt adjoint) can
-    differ."""
+    sources, limiter cases, recorded HLLC solves) gives the gradient of the
+    reverse step that recomputes them: the same values enter the same reverse
+    arithmetic, so only the order of additions (J, ghost folding, dt
+    adjoint) can differ."""
     p = e2d.make_params(nx=96, ny=80, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
                         boundary_type_xmax=2, boundary_type_ymin=3, boundary_type_ymax=3)
     po = oracle.Params(nx=96, ny=80, gamma0=1.4, cfl=0.8, riemann=2, bc_xmax=2, bc_ymin=3, bc_ymax=3)
-    u0 = smooth_base(oracle, po)
+    # (the FMA build's reverse without a tape recomputes its face states in
+    # the exact form, a rounding away from its forward's: a state without
+    # near-ties keeps the branches the same)
+    u0 = smooth_base(oracle, po) if arith == "exact" else generic_base(oracle, po)
     n = 31  # K = 6, a ragged last segment
-    with e2d.Adjoint(p) as a:
+    with e2d.Adjoint(p, arith=arith) as a:
         J1, g1, d1 = a.gradient(n, u0, dt_mode=dt_mode)
     monkeypatch.setenv("E2D_NO_TAPE", "1")
-    with e2d.Adjoint(p) as b:
+    with e2d.Adjoint(p, arith=arith) as b:
         J2, g2, d2 = b.gradient(n, u0, dt_mode=dt_mode)
     assert np.array_equal(d1, d2)
     assert abs(J1 - J2) <= 1e-13 * abs(J2)  # J is summed with atomic additions
