@@ -447,7 +447,7 @@ int e2d_batch_tune(e2d_batch* b, int steps, const char* cache_path, float* best_
   int bv = b->variant, bm = b->mult, bo = b->order;
   int rc = E2D_OK;
   for (int v = 0; v <= 1 && rc == E2D_OK; ++v)
-    for (int m : {1, 2, 4})
+    for (int m : {1, 2, 3, 4})
       for (int o = 0; o <= 1 && rc == E2D_OK; ++o) {
         if ((rc = e2d_batch_set_schedule(b, v, m, o))) break;
         float ms = 0;

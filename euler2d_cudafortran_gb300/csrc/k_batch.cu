@@ -103,17 +103,19 @@ __global__ void __launch_bounds__(C::NT, MINB)
     Field<Real> out{parity ? P.u : P.u2, P.pitch, P.plane};
     const Field<Real> qout{QIN ? (parity ? P.q : P.q2) : out.p, P.pitch, P.plane};
     const int next = t + gridDim.x;
+    // thread 0 finds the next tile's problem at the start of the face phase,
+    // where warps claim faces dynamically and no barrier waits for it; the
+    // barrier that ends the face phase publishes nxt to the prefetch
+    auto find_next = [&]() {
+      if (tid == 0 && next < total_tiles) lookup(next, nxt);
+    };
     auto prefetch = [&]() {  // every thread, right after the face phase
-      if (next < total_tiles) {
-        if (tid == 0) lookup(next, nxt);
-        __syncthreads();
-        issue(nxt, dreg);
-      }
+      if (next < total_tiles) issue(nxt, dreg);
     };
     const bool only = TAPE && P.tape.only;  // a tape-only pass: no update, no dt
     Real m = tile_compute<Real, C, SQ, QIN, TAPE>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1],
                                                   sdt[2], true, wr >= 0 && !only, &ctls[id].health,
-                                                  (QIN || first) ? nullptr : dreg, prefetch, &P.tape);
+                                                  (QIN || first) ? nullptr : dreg, prefetch, &P.tape, find_next);
     if (tid == 0 && !only) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];

@@ -194,7 +194,13 @@ __device__ __forceinline__ void primitives(const Hydro<Real>& h, const Real u[4]
   q[ID] = O::max(u[ID], h.smallr);
   q[IU] = O::div(u[IU], q[ID]);
   q[IV] = O::div(u[IV], q[ID]);
+#if E2D_FMA_FORMS
+  // a sum of two products written as one fused form, so that every kernel
+  // rounds it alike (contraction alone may fuse either product)
+  const Real eken = O::half(fmx(q[IU], q[IU], q[IV] * q[IV]));
+#else
   const Real eken = O::half((q[IU] * q[IU]) + (q[IV] * q[IV]));
+#endif
   const Real e = O::div(u[IP], q[ID]) - eken;
   q[IP] = floor_prod((h.gm1 * q[ID]) * e, q[ID], h.smallp);
 }
@@ -344,10 +350,23 @@ __device__ __forceinline__ void trace_sources(const Hydro<Real>& h, const Real q
                                               const Real dqy[4], Real s[4]) {
   using O = Ops<Real>;
   const Real r = q[ID], p = q[IP], u = q[IU], v = q[IV];
+#if E2D_FMA_FORMS
+  // s = -(u*dqx + v*dqy + t) as one fused form (the form of trace_qs), so
+  // that every kernel rounds it alike
+  const Real dv = dqx[IU] + dqy[IV];
+  Real t[4];
+  t[ID] = dv * r;
+  t[IP] = (dv * h.gamma0) * p;
+  t[IU] = O::div(dqx[IP], r);
+  t[IV] = O::div(dqy[IP], r);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) s[k] = O::neg_if(fmx(u, dqx[k], fmx(v, dqy[k], t[k])), true);
+#else
   s[ID] = ((-(u * dqx[ID])) - (v * dqy[ID])) - ((dqx[IU] + dqy[IV]) * r);
   s[IP] = ((-(u * dqx[IP])) - (v * dqy[IP])) - (((dqx[IU] + dqy[IV]) * h.gamma0) * p);
   s[IU] = ((-(u * dqx[IU])) - (v * dqy[IU])) - O::div(dqx[IP], r);
   s[IV] = ((-(u * dqx[IV])) - (v * dqy[IV])) - O::div(dqy[IP], r);
+#endif
 }
 
 // The FMA build's cell value for its four face states on square cells:
@@ -402,7 +421,11 @@ __device__ __forceinline__ void cmpflx(const Hydro<Real>& h, const Real qg[4], R
   flux[ID] = qg[ID] * qg[IU];
   flux[IU] = (flux[ID] * qg[IU]) + qg[IP];
   flux[IV] = flux[ID] * qg[IV];
+#if E2D_FMA_FORMS
+  const Real ekin = O::half(qg[ID]) * fmx(qg[IU], qg[IU], qg[IV] * qg[IV]);
+#else
   const Real ekin = O::half(qg[ID]) * ((qg[IU] * qg[IU]) + (qg[IV] * qg[IV]));
+#endif
   const Real etot = (qg[IP] * h.entho) + ekin;
   flux[IP] = qg[IU] * (etot + qg[IP]);
 }
@@ -424,7 +447,11 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
   const Real cr = (h.gamma0 * pr) * rr;
   Real wl = O::sqrt(cl);
   Real wr = O::sqrt(cr);
+#if E2D_FMA_FORMS
+  Real pold = O::max(O::div(fmx(wr, pl, fmx(wl, pr, (wl * wr) * (ul - ur))), wl + wr), ZERO);
+#else
   Real pold = O::max(O::div(((wr * pl) + (wl * pr)) + ((wl * wr) * (ul - ur)), wl + wr), ZERO);
+#endif
   Real conv = ONE;
   int iter = 0;
   while (iter < h.niter_riemann && O::gt(conv, tol)) {
@@ -458,9 +485,16 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
   const Real scr = O::max(spout - spin, h.smallc + rabs(spout + spin));
   const Real frac = O::half(ONE + O::div(spout + spin, scr));
   Real qg[4];
+#if E2D_FMA_FORMS
+  const Real gfrac = ONE - frac;
+  qg[ID] = fmx(frac, rstar, gfrac * ro);
+  qg[IU] = fmx(frac, ustar, gfrac * uo);
+  qg[IP] = fmx(frac, pstar, gfrac * po);
+#else
   qg[ID] = (frac * rstar) + ((ONE - frac) * ro);
   qg[IU] = (frac * ustar) + ((ONE - frac) * uo);
   qg[IP] = (frac * pstar) + ((ONE - frac) * po);
+#endif
   if (O::lt0(spout)) { qg[ID] = ro; qg[IU] = uo; qg[IP] = po; }
   if (O::gt0(spin)) { qg[ID] = rstar; qg[IU] = ustar; qg[IP] = pstar; }
   qg[IV] = left ? qleft[IV] : qright[IV];
@@ -511,6 +545,25 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
 #endif
   Real ro, uo, ptoto, etoto;
+#if E2D_FMA_FORMS
+  // the star states reuse rcl = rl (ul - SL) and rcr = rr (SR - ur):
+  // rl (SL - ul) / (SL - ustar) = rcl / (ustar - SL), and so on
+  if (O::gt0(SL)) {
+    ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
+  } else if (O::gt0(ustar)) {
+    const Real d = ustar - SL;
+    ro = O::div(rcl, d);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div(fmx(ul - SL, etotl, fmx(ptotl, ul, -(ptotstar * ustar))), d);
+  } else if (O::gt0(SR)) {
+    const Real d = SR - ustar;
+    ro = O::div(rcr, d);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div(fmx(SR - ur, etotr, fmx(-ptotr, ur, ptotstar * ustar)), d);
+  } else {
+    ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
+  }
+#else
   if (O::gt0(SL)) {
     ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
   } else if (O::gt0(ustar)) {
@@ -524,6 +577,7 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   } else {
     ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
   }
+#endif
   flux[ID] = ro * uo;
   flux[IU] = ((ro * uo) * uo) + ptoto;
   flux[IP] = (etoto + ptoto) * uo;
@@ -593,6 +647,23 @@ __device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const d
 #endif
   double ro, uo, ptoto, etoto;
   const bool b1 = O::gt0(SL), b2 = !b1 && O::gt0(ustar), b3 = !b1 && !b2 && O::gt0(SR);
+#if E2D_FMA_FORMS
+  if (b1) {
+    ro = rl; uo = ul; ptoto = pl; etoto = etotl;
+  } else if (b2) {
+    const double d = ustar - SL;
+    ro = O::div(rcl, d);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div(fmx(ul - SL, etotl, fmx(pl, ul, -(ptotstar * ustar))), d);
+  } else if (b3) {
+    const double d = SR - ustar;
+    ro = O::div(rcr, d);
+    uo = ustar; ptoto = ptotstar;
+    etoto = O::div(fmx(SR - ur, etotr, fmx(-pr, ur, ptotstar * ustar)), d);
+  } else {
+    ro = rr; uo = ur; ptoto = pr; etoto = etotr;
+  }
+#else
   if (b1) {
     ro = rl; uo = ul; ptoto = pl; etoto = etotl;
   } else if (b2) {
@@ -606,6 +677,7 @@ __device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const d
   } else {
     ro = rr; uo = ur; ptoto = pr; etoto = etotr;
   }
+#endif
   const double f0 = ro * uo;
   const bool vleft = O::gt0(f0);
 #pragma unroll

@@ -84,12 +84,17 @@ __device__ __forceinline__ bool owns(int g, int t0, int w, int n) {
 // function of its conservative values, so this changes no result.
 // TAPE (FP64, !QIN): the step also writes its input's forward values to
 // *tape (TapeOut).
-template <typename Real, class C, bool SQ = false, bool QIN = false, bool TAPE = false, class Hook = NoHook>
+// before_faces: run by every thread right after the barrier that ends the
+// ring pass, before it claims faces (work there delays no barrier: the faces
+// are claimed dynamically).
+template <typename Real, class C, bool SQ = false, bool QIN = false, bool TAPE = false, class Hook = NoHook,
+          class Hook2 = NoHook>
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
                                              int i0, int j0, const Field<Real>& in, const Field<Real>& out,
                                              const Field<Real>& qout, Real dtdx, Real dtdy, bool fill_ghosts,
                                              bool want_dt, unsigned* health, const Real* box_src = nullptr,
-                                             Hook after_faces = Hook(), const TapeOut* tape = nullptr) {
+                                             Hook after_faces = Hook(), const TapeOut* tape = nullptr,
+                                             Hook2 before_faces = Hook2()) {
   static_assert(!TAPE || (sizeof(Real) == 8 && !QIN), "the tape is written by the FP64 conversion path");
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, BXs = C::BXs, BYs = C::BYs, RX = C::RX, RY = C::RY;
   Real* sq = base + C::q_off;
@@ -187,6 +192,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1);
   constexpr int Y0 = (NXF + 31) / 32 * 32, NF = Y0 + NYF;
   const int lane = tid & 31;
+  before_faces();
   while (true) {
     int chunk = 0;
     if (lane == 0) chunk = atomicAdd(face_counter, 32);
