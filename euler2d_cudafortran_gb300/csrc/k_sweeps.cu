@@ -252,6 +252,19 @@ __global__ void k_trace_v1(Hydro<Real> h, Field<Real> q, StepDt<Real> sd, Ctl* c
   Real qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4], f[4];
   load4(q, j, i, qc); load4(q, j, i + 1, qe); load4(q, j, i - 1, qw); load4(q, j + 1, i, qn); load4(q, j - 1, i, qs);
   slopes(h, qc, qe, qw, qn, qs, dqx, dqy);
+#if E2D_FMA_FORMS
+  // the FMA build on square cells: qs = q + (s*dtdx)*0.5 in fused steps,
+  // each face state one fused multiply-add per variable (as the fused step)
+  if (h.dx == h.dy) {
+    Real qsrc[4];
+    trace_qs(h, qc, dqx, dqy, Ops<Real>::half(dtdx), qsrc);
+    trace_face_qs<Real, false>(h, qsrc, dqx, f); store4(qxm, j, i, f);
+    trace_face_qs<Real, true>(h, qsrc, dqx, f);  store4(qxp, j, i, f);
+    trace_face_qs<Real, false>(h, qsrc, dqy, f); store4(qym, j, i, f);
+    trace_face_qs<Real, true>(h, qsrc, dqy, f);  store4(qyp, j, i, f);
+    return;
+  }
+#endif
   trace_sources(h, qc, dqx, dqy, s);
   // FP64 with dtdx == dtdy: the source term (s*dtd)*0.5 is the same for the
   // four faces (+0.8 %; the FP32 build, not bound by its FP pipes, is left as it is)
@@ -293,6 +306,9 @@ __global__ void __launch_bounds__(V1_NT) k_flux_update_v1(Hydro<Real> h, Field<R
   const Real dt = resolve_dt(h, sd, ctl);
   const Real dtdx = Ops<Real>::div(dt, h.dx);
   const Real dtdy = Ops<Real>::div(dt, h.dy);
+  // the FMA build on square cells keeps the raw fluxes and fuses dt/dx into
+  // the update (as the fused step)
+  const bool raw = E2D_FMA_FORMS && h.dx == h.dy;
   for (int k = tid; k < NF; k += NT) {
     if (k < NXF) {
       // x-faces: face f (0..TX) of row r sits between cells i0+f-1 and i0+f
@@ -304,7 +320,7 @@ __global__ void __launch_bounds__(V1_NT) k_flux_update_v1(Hydro<Real> h, Field<R
         load4(qxm, j, i, qr);
         riemann(h, ql, qr, flux);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sfx[v][r][f] = flux[v] * dtdx;
+        for (int v = 0; v < 4; ++v) sfx[v][r][f] = raw ? flux[v] : flux[v] * dtdx;
       }
     } else if (k >= Y0) {
       // y-faces: face g (0..TY) of column c sits between cells j0+g-1 and j0+g
@@ -319,7 +335,7 @@ __global__ void __launch_bounds__(V1_NT) k_flux_update_v1(Hydro<Real> h, Field<R
         riemann(h, ql, qr, flux);
         t = flux[IU]; flux[IU] = flux[IV]; flux[IV] = t;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sfy[v][g][c] = flux[v] * dtdy;
+        for (int v = 0; v < 4; ++v) sfy[v][g][c] = raw ? flux[v] : flux[v] * dtdy;
       }
     }
   }
@@ -333,7 +349,7 @@ __global__ void __launch_bounds__(V1_NT) k_flux_update_v1(Hydro<Real> h, Field<R
     for (int v = 0; v < 4; ++v) {
       Real flux_tot = sfx[v][r][c] - sfx[v][r][c + 1];
       flux_tot = (sfy[v][r][c] - sfy[v][r + 1][c]) + flux_tot;
-      un[v] = in.at(v, j, i) + flux_tot;
+      un[v] = raw ? fmx(flux_tot, dtdx, in.at(v, j, i)) : in.at(v, j, i) + flux_tot;
       out.at(v, j, i) = un[v];
     }
     m = new_state_checks(h, i, j, un, ctl, sd.wr_slot >= 0);
