@@ -79,6 +79,8 @@ struct e2d_run {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
   bool download_pending = false;
+  // pinned host word for compute_dt's read-back of the running maximum
+  double* h_inv = nullptr;
 };
 
 namespace {
@@ -211,8 +213,10 @@ void enqueue_percall_q(e2d_run* r, int nStep, Real dt) {
   const int b = nStep % 2;
   {
     NvtxRange rg(NVTX_BOUNDARIES);
-    launch_boundaries<Real>(h, field<Real>(r, b ? r->u2 : r->u), r->stream);
-    if (r->q_valid[b]) launch_boundaries<Real>(h, field<Real>(r, r->qprim[b]), r->stream);
+    if (r->q_valid[b])
+      launch_boundaries_pair<Real>(h, field<Real>(r, b ? r->u2 : r->u), field<Real>(r, r->qprim[b]), r->stream);
+    else
+      launch_boundaries<Real>(h, field<Real>(r, b ? r->u2 : r->u), r->stream);
   }
   if (!r->q_valid[b]) {
     NvtxRange rg(NVTX_PRIMITIVES);
@@ -224,10 +228,12 @@ void enqueue_percall_q(e2d_run* r, int nStep, Real dt) {
 
 template <typename Real>
 int finish_dt(e2d_run* r, void* dt_out) {
-  Real inv;
-  E2D_CK(cudaMemcpyAsync(&inv, inv_slot<Real>(r->ctl, r->cur_slot), sizeof(Real), cudaMemcpyDeviceToHost,
+  Real inv_local;
+  Real* hp = r->h_inv ? reinterpret_cast<Real*>(r->h_inv) : &inv_local;  // pinned: a direct copy
+  E2D_CK(cudaMemcpyAsync(hp, inv_slot<Real>(r->ctl, r->cur_slot), sizeof(Real), cudaMemcpyDeviceToHost,
                          r->stream));
   E2D_CK(cudaStreamSynchronize(r->stream));
+  const Real inv = *hp;
   const Real dt = hydro<Real>(r).cfl / inv;
   *static_cast<Real*>(dt_out) = dt;
   return E2D_OK;
@@ -336,6 +342,10 @@ int e2d_create(const e2d_params* p, e2d_run** out) {
       cudaEventCreate(&r->ev0) != cudaSuccess || cudaEventCreate(&r->ev1) != cudaSuccess)
     return cleanup(E2D_ERR_CUDA, "stream/event creation failed");
   r->stream = r->own_stream;
+  if (cudaMallocHost(&r->h_inv, sizeof(double)) != cudaSuccess) {  // optional: a pageable copy otherwise
+    cudaGetLastError();
+    r->h_inv = nullptr;
+  }
   cudaMemsetAsync(r->u, 0, sb, r->stream);
   cudaMemsetAsync(r->u2, 0, sb, r->stream);
   for (int k = 0; k < nwork; ++k) cudaMemsetAsync(r->work[k], 0, sb, r->stream);
@@ -389,6 +399,7 @@ int e2d_destroy(e2d_run* r) {
   if (r->ev_snap) cudaEventDestroy(r->ev_snap);
   if (r->ev_copied) cudaEventDestroy(r->ev_copied);
   cudaFree(r->snapshot);
+  if (r->h_inv) cudaFreeHost(r->h_inv);
   if (r->own_stream) cudaStreamDestroy(r->own_stream);
   delete r;
   return E2D_OK;
@@ -542,11 +553,13 @@ int e2d_make_boundaries(e2d_run* r, int which) {
   if (int rc = check_run(r)) return rc;
   if (which != 0 && which != 1) return fail(E2D_ERR_INVALID_ARG, "which must be 0 (u) or 1 (u2)");
   if (int rc = use_device(r)) return rc;
-  if (r->es == 8) launch_boundaries<double>(r->hd, field<double>(r, which ? r->u2 : r->u), r->stream);
-  else launch_boundaries<float>(r->hf, field<float>(r, which ? r->u2 : r->u), r->stream);
-  if (r->q_valid[which]) {  // the primitives' ghosts follow (a flipped momentum is a flipped velocity)
-    if (r->es == 8) launch_boundaries<double>(r->hd, field<double>(r, r->qprim[which]), r->stream);
-    else launch_boundaries<float>(r->hf, field<float>(r, r->qprim[which]), r->stream);
+  // the primitives' ghosts follow in the same launch (a flipped momentum is a flipped velocity)
+  if (r->es == 8) {
+    const Field<double> w = field<double>(r, r->q_valid[which] ? r->qprim[which] : nullptr);
+    launch_boundaries_pair<double>(r->hd, field<double>(r, which ? r->u2 : r->u), w, r->stream);
+  } else {
+    const Field<float> w = field<float>(r, r->q_valid[which] ? r->qprim[which] : nullptr);
+    launch_boundaries_pair<float>(r->hf, field<float>(r, which ? r->u2 : r->u), w, r->stream);
   }
   E2D_CK(cudaGetLastError());
   return E2D_OK;

@@ -88,9 +88,12 @@ __global__ void k_init_diagonal(Hydro<Real> h, Field<Real> u, double offset, dou
 
 // make_boundaries, serial_ref/m_run.f90:561-648.  One thread per ghost cell of
 // the 4 edges (x edges over interior rows, y edges over interior columns);
-// the corner blocks are never written.
+// the corner blocks are never written.  w (when w.p is set): a second array
+// of the same layout filled by the same rules in the same launch (the
+// primitives kept beside a state: a reflective wall's flipped momentum is a
+// flipped velocity).
 template <typename Real>
-__global__ void k_boundaries(Hydro<Real> h, Field<Real> u) {
+__global__ void k_boundaries(Hydro<Real> h, Field<Real> u, Field<Real> w) {
   const int nx = h.nx, ny = h.ny;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nxe = 4 * ny, nye = 4 * nx;
@@ -108,6 +111,7 @@ __global__ void k_boundaries(Hydro<Real> h, Field<Real> u) {
     for (int v = 0; v < 4; ++v) {
       const Real dir = (type == 1 && v == IU) ? Real(-1.0) : Real(1.0);
       u.at(v, j, i) = u.at(v, j, i0) * dir;
+      if (w.p) w.at(v, j, i) = w.at(v, j, i0) * dir;
     }
   } else if (t < nxe + nye) {
     const int tt = t - nxe;
@@ -124,6 +128,7 @@ __global__ void k_boundaries(Hydro<Real> h, Field<Real> u) {
     for (int v = 0; v < 4; ++v) {
       const Real dir = (type == 1 && v == IV) ? Real(-1.0) : Real(1.0);
       u.at(v, j, i) = u.at(v, j0, i) * dir;
+      if (w.p) w.at(v, j, i) = w.at(v, j0, i) * dir;
     }
   }
 }
@@ -370,7 +375,13 @@ void launch_init_diagonal(const Hydro<Real>& h, Field<Real> u, double offset, do
 template <typename Real>
 void launch_boundaries(const Hydro<Real>& h, Field<Real> u, cudaStream_t s) {
   const long long n = 4LL * h.nx + 4LL * h.ny;
-  k_boundaries<Real><<<cdiv(n, 256), 256, 0, s>>>(h, u);
+  k_boundaries<Real><<<cdiv(n, 256), 256, 0, s>>>(h, u, Field<Real>{nullptr, 0, 0});
+}
+
+template <typename Real>
+void launch_boundaries_pair(const Hydro<Real>& h, Field<Real> u, Field<Real> w, cudaStream_t s) {
+  const long long n = 4LL * h.nx + 4LL * h.ny;
+  k_boundaries<Real><<<cdiv(n, 256), 256, 0, s>>>(h, u, w);
 }
 
 template <typename Real>
@@ -420,6 +431,7 @@ void launch_flux_update_v1(const Hydro<Real>& h, Field<Real> in, Field<Real> qxm
   template void launch_init_diagonal<Real>(const Hydro<Real>&, Field<Real>, double, double, double, double,    \
                                            double, cudaStream_t);                                              \
   template void launch_boundaries<Real>(const Hydro<Real>&, Field<Real>, cudaStream_t);                        \
+  template void launch_boundaries_pair<Real>(const Hydro<Real>&, Field<Real>, Field<Real>, cudaStream_t);      \
   template void launch_dt_reduce<Real>(const Hydro<Real>&, Field<Real>, Ctl*, int, cudaStream_t);              \
   template void launch_prim<Real>(const Hydro<Real>&, Field<Real>, Field<Real>, cudaStream_t);                 \
   template void launch_fluxes_v2<Real>(const Hydro<Real>&, Field<Real>, StepDt<Real>, Ctl*, Field<Real>,       \

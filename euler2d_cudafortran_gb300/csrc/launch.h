@@ -45,6 +45,9 @@ int set_error(int code, const std::string& msg);
 template <typename Real> void launch_init_diagonal(const Hydro<Real>& h, Field<Real> u, double offset, double rho_hi,
                                                    double p_hi, double rho_lo, double p_lo, cudaStream_t s);
 template <typename Real> void launch_boundaries(const Hydro<Real>& h, Field<Real> u, cudaStream_t s);
+// make_boundaries on u and, in the same launch, on w (same layout and rules).
+template <typename Real>
+void launch_boundaries_pair(const Hydro<Real>& h, Field<Real> u, Field<Real> w, cudaStream_t s);
 // Reduce the CFL maximum of u into ctl->inv[slot] (atomic max; running max kept).
 template <typename Real> void launch_dt_reduce(const Hydro<Real>& h, Field<Real> u, Ctl* ctl, int slot, cudaStream_t s);
 template <typename Real> void launch_prim(const Hydro<Real>& h, Field<Real> u, Field<Real> q, cudaStream_t s);

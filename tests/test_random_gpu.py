@@ -74,3 +74,30 @@ def test_random_adjoint_matches_tangent(e2d, oracle, k, dt_mode):
     Jt, dJt = oracle.tangent(po, u0, d, c["nsteps"], nthreads=NTHREADS, fixed_dts=dts if dt_mode == 0 else None)
     assert abs(J - Jt) <= 1e-13 * abs(Jt)
     assert abs(float(np.sum(g * d)) - dJt) <= 1e-9 * abs(dJt), (c, float(np.sum(g * d)), dJt)
+
+
+def _rel_l1(gpu, ref):
+    """Relative L1 difference per conservative variable (interior cells); a
+    variable whose oracle values nearly vanish is measured against 1e-9 of
+    the density's L1 instead."""
+    a, b = gpu[:, 2:-2, 2:-2].astype(np.float64), ref[:, 2:-2, 2:-2].astype(np.float64)
+    floor = 1e-9 * float(np.abs(b[0]).sum())
+    return [float(np.abs(a[v] - b[v]).sum() / max(np.abs(b[v]).sum(), floor)) for v in range(4)]
+
+
+@pytest.mark.parametrize("k", range(len(CASES)))
+def test_random_configuration_fma_build(e2d, oracle, k):
+    """The same thirty configurations with the build that fuses multiply-adds:
+    FP64 within 1e-12 relative L1 per variable and 1e-14 relative dt of the
+    oracle, FP32 within 1e-5 of the FP32 oracle, every implementation version."""
+    c = CASES[k]
+    for prec, (l1_tol, dt_tol) in ((8, (1e-12, 1e-14)), (4, (1e-5, 1e-5))):
+        for version in (0, 1, 2):
+            pe, po = _params(e2d, oracle, c, version, prec)
+            prec_s = "f64" if prec == 8 else "f32"
+            u0 = oracle.init_diagonal(po, c["offset"], c["rho_hi"], c["p_hi"], c["rho_lo"], c["p_lo"], prec=prec_s)
+            ref, dts_ref, _, _ = oracle.run(po, c["nsteps"], prec=prec_s, u0=u0, nthreads=NTHREADS)
+            gpu, dts = e2d.run_steps(c["nsteps"], pe, u0=u0, arith="fma")
+            l1 = _rel_l1(gpu, ref)
+            dr = float(np.max(np.abs(dts.astype(np.float64) - dts_ref) / np.abs(dts_ref)))
+            assert max(l1) <= l1_tol and dr <= dt_tol, (c, version, prec, l1, dr)
