@@ -226,6 +226,24 @@ void enqueue_percall_q(e2d_run* r, int nStep, Real dt) {
   r->q_valid[0] = r->q_valid[1] = true;
 }
 
+// The device address of `bytes` of host memory the GPU can read and write
+// directly (pinned and mapped: cudaMallocHost / cudaHostAlloc /
+// e2d_host_alloc, torch's pin_memory), or null when the memory is pageable
+// or the pinned mapping does not cover the last byte as well.
+const void* mapped_host(const void* host, size_t bytes) {
+  cudaPointerAttributes a, b;
+  const char* last = static_cast<const char*>(host) + (bytes - 1);
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess || cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer)
+    return nullptr;
+  if (static_cast<const char*>(b.devicePointer) != static_cast<const char*>(a.devicePointer) + (bytes - 1))
+    return nullptr;
+  return a.devicePointer;
+}
+
 template <typename Real>
 int finish_dt(e2d_run* r, void* dt_out) {
   Real inv_local;
@@ -458,8 +476,13 @@ int e2d_upload_state(e2d_run* r, int which, const void* host) {
   const size_t w = (size_t)r->isize * r->es;
   r->folded[which] = false;
   r->q_valid[which] = false;
-  E2D_CK(cudaMemcpy2DAsync(which ? r->u2 : r->u, r->pitch * r->es, host, w, w, (size_t)4 * r->jsize,
-                           cudaMemcpyHostToDevice, r->stream));
+  if (const void* hd = mapped_host(host, w * 4 * r->jsize)) {  // pinned: rows repitched at the link's rate
+    launch_repitch(hd, (size_t)r->isize, which ? r->u2 : r->u, r->pitch, r->isize, 4 * r->jsize, r->es, r->stream);
+    E2D_CK(cudaGetLastError());
+  } else {
+    E2D_CK(cudaMemcpy2DAsync(which ? r->u2 : r->u, r->pitch * r->es, host, w, w, (size_t)4 * r->jsize,
+                             cudaMemcpyHostToDevice, r->stream));
+  }
   E2D_CK(cudaStreamSynchronize(r->stream));
   return E2D_OK;
 }
@@ -469,8 +492,13 @@ int e2d_download_state(e2d_run* r, int which, void* host) {
   if (!host || (which != 0 && which != 1)) return fail(E2D_ERR_INVALID_ARG, "bad download arguments");
   if (int rc = use_device(r)) return rc;
   const size_t w = (size_t)r->isize * r->es;
-  E2D_CK(cudaMemcpy2DAsync(host, w, which ? r->u2 : r->u, r->pitch * r->es, w, (size_t)4 * r->jsize,
-                           cudaMemcpyDeviceToHost, r->stream));
+  if (void* hd = const_cast<void*>(mapped_host(host, w * 4 * r->jsize))) {
+    launch_repitch(which ? r->u2 : r->u, r->pitch, hd, (size_t)r->isize, r->isize, 4 * r->jsize, r->es, r->stream);
+    E2D_CK(cudaGetLastError());
+  } else {
+    E2D_CK(cudaMemcpy2DAsync(host, w, which ? r->u2 : r->u, r->pitch * r->es, w, (size_t)4 * r->jsize,
+                             cudaMemcpyDeviceToHost, r->stream));
+  }
   E2D_CK(cudaStreamSynchronize(r->stream));
   return E2D_OK;
 }

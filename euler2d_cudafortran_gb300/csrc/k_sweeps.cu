@@ -372,6 +372,37 @@ void launch_init_diagonal(const Hydro<Real>& h, Field<Real> u, double offset, do
   k_init_diagonal<Real><<<g, b, 0, s>>>(h, u, offset, rho_hi, p_hi, rho_lo, p_lo);
 }
 
+namespace {
+
+// Row copy between a packed array (rows of `width` words, e.g. a host state
+// in the Fortran layout, read or written through its mapped address) and a
+// pitched one: row r of `rows`, word c.  Consecutive threads take
+// consecutive words of a row.
+template <typename Word>
+__global__ void k_repitch(const Word* __restrict__ src, long long src_pitch, Word* __restrict__ dst,
+                          long long dst_pitch, int width, int rows) {
+  const long long n = (long long)width * rows;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const long long r = k / width, c = k - r * width;
+    dst[r * dst_pitch + c] = src[r * src_pitch + c];
+  }
+}
+
+}  // namespace
+
+void launch_repitch(const void* src, size_t src_pitch, void* dst, size_t dst_pitch, int width, int rows,
+                    int word_bytes, cudaStream_t s) {
+  const long long n = (long long)width * rows;
+  const int grid = (int)std::min<long long>(cdiv(n, 256), 152LL * 8);
+  if (word_bytes == 8)
+    k_repitch<unsigned long long><<<grid, 256, 0, s>>>(static_cast<const unsigned long long*>(src), (long long)src_pitch,
+                                                       static_cast<unsigned long long*>(dst), (long long)dst_pitch,
+                                                       width, rows);
+  else
+    k_repitch<unsigned int><<<grid, 256, 0, s>>>(static_cast<const unsigned int*>(src), (long long)src_pitch,
+                                                 static_cast<unsigned int*>(dst), (long long)dst_pitch, width, rows);
+}
+
 template <typename Real>
 void launch_boundaries(const Hydro<Real>& h, Field<Real> u, cudaStream_t s) {
   const long long n = 4LL * h.nx + 4LL * h.ny;

@@ -45,6 +45,11 @@ int set_error(int code, const std::string& msg);
 template <typename Real> void launch_init_diagonal(const Hydro<Real>& h, Field<Real> u, double offset, double rho_hi,
                                                    double p_hi, double rho_lo, double p_lo, cudaStream_t s);
 template <typename Real> void launch_boundaries(const Hydro<Real>& h, Field<Real> u, cudaStream_t s);
+// Row copy between pitched arrays of 4- or 8-byte words (pitches in words);
+// either side may be mapped pinned host memory (copies at the host link's
+// rate without a staging buffer).
+void launch_repitch(const void* src, size_t src_pitch, void* dst, size_t dst_pitch, int width, int rows,
+                    int word_bytes, cudaStream_t s);
 // make_boundaries on u and, in the same launch, on w (same layout and rules).
 template <typename Real>
 void launch_boundaries_pair(const Hydro<Real>& h, Field<Real> u, Field<Real> w, cudaStream_t s);

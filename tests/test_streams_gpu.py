@@ -111,3 +111,33 @@ def test_kept_primitives_change_no_bit(e2d, monkeypatch, prec):
             runs.append((r.get_state(1), dts))
     assert np.array_equal(runs[0][0], runs[1][0])
     assert np.array_equal(runs[0][1], runs[1][1])
+
+
+@pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
+@pytest.mark.parametrize("nx", [96, 33], ids=["even", "odd"])
+def test_pinned_host_arrays_copy_like_pageable_ones(e2d, prec, nx):
+    """Upload and download through pinned (mapped) host memory, which the
+    library copies with a kernel reading or writing the host rows directly,
+    move the same bytes as through pageable memory (the 2D copy), for even
+    and odd row lengths; rows of a pinned array past the state are left
+    alone."""
+    torch = pytest.importorskip("torch")
+    p = e2d.make_params(nx=nx, ny=40, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC, precision=prec)
+    dt = np.float64 if prec == 8 else np.float32
+    rng = np.random.default_rng(5)
+    with e2d.HydroRun(p) as run:
+        shape = (4, run.jsize, run.isize)
+        src = rng.uniform(0.5, 2.0, size=shape).astype(dt)
+        pinned = torch.empty(int(np.prod(shape)) + 64, dtype=torch.float64 if prec == 8 else torch.float32,
+                             pin_memory=True).numpy()
+        pinned[:] = -3.0
+        pin_state = pinned[: np.prod(shape)].reshape(shape)
+        pin_state[...] = src
+        run.set_state(0, pin_state)          # pinned upload
+        run.set_state(1, src)                # pageable upload
+        a = run.get_state(0)                 # pageable download
+        pin_state[...] = 0.0
+        run.get_state(1, out=pin_state)      # pinned download
+        assert np.array_equal(a, src)
+        assert np.array_equal(pin_state, src)
+        assert np.all(pinned[np.prod(shape):] == -3.0)
