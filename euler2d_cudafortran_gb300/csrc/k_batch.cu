@@ -41,10 +41,8 @@ __global__ void __launch_bounds__(C::NT, MINB)
   unsigned char* tail = reinterpret_cast<unsigned char*>(base + C::n_real);
   int* face_counter = reinterpret_cast<int*>(tail + 8);
   Real* red = reinterpret_cast<Real*>(tail + 16);
-  // the current tile's problem parameters and dt (dt, dt/dx, dt/dy) in one
-  // half, the next tile's (fetched during the face phase) in the other
-  __shared__ Hydro<Real> shb[2];
-  __shared__ Real sdtb[2][3];
+  Real* sdt = red + 32;
+  __shared__ Hydro<Real> sh;
   __shared__ int cur[3], nxt[3];  // problem (work-list order), problem index, tile within the problem
   const int tid = threadIdx.x;
   Real* const dreg = QIN ? base + C::q_off : base + C::d_off;  // where a prefetched box lands
@@ -81,31 +79,23 @@ __global__ void __launch_bounds__(C::NT, MINB)
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
 
-  auto params = [&](const int* info, int half) {  // thread 0: the problem's parameters and dt
-    Hydro<Real>& hp = shb[half];
-    hp = probs[info[0]].h;
-    const Real dt0 = dt_src ? dt_src[info[1]] : hp.cfl / *inv_slot<Real>(&ctls[info[1]], rd);
-    sdtb[half][0] = dt0;
-    sdtb[half][1] = dt0 / hp.dx;
-    sdtb[half][2] = dt0 / hp.dy;
-  };
-
   int t = blockIdx.x;
   if (t >= total_tiles) return;
-  int half = 0;
-  if (tid == 0) {
-    lookup(t, cur);
-    params(cur, half);
-  }
+  if (tid == 0) lookup(t, cur);
   __syncthreads();
   issue(cur, base + C::q_off);
   bool first = true;
   for (; t < total_tiles; t += gridDim.x) {
-    if (tid == 0) *face_counter = 0;
+    if (tid == 0) {
+      sh = probs[cur[0]].h;
+      *face_counter = 0;
+      const Real dt0 = dt_src ? dt_src[cur[1]] : sh.cfl / *inv_slot<Real>(&ctls[cur[1]], rd);
+      sdt[0] = dt0;
+      sdt[1] = dt0 / sh.dx;
+      sdt[2] = dt0 / sh.dy;
+    }
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();  // every thread's copies, the problem's parameters and dt
-    const Hydro<Real>& sh = shb[half];
-    const Real* sdt = sdtb[half];
     const int p = cur[0], id = cur[1], stile = cur[2];
     const BatchProb<Real>& P = probs[p];
     const int i0 = GW + (stile % P.ntx) * C::TX, j0 = GW + (stile / P.ntx) * C::TY;
@@ -113,15 +103,11 @@ __global__ void __launch_bounds__(C::NT, MINB)
     Field<Real> out{parity ? P.u : P.u2, P.pitch, P.plane};
     const Field<Real> qout{QIN ? (parity ? P.q : P.q2) : out.p, P.pitch, P.plane};
     const int next = t + gridDim.x;
-    // thread 0 finds the next tile's problem, its parameters and dt at the
-    // start of the face phase, where warps claim faces dynamically and no
-    // barrier waits for it; the barrier that ends the face phase publishes
-    // them (nxt to the prefetch, the other half of shb / sdtb to the next tile)
+    // thread 0 finds the next tile's problem at the start of the face phase,
+    // where warps claim faces dynamically and no barrier waits for it; the
+    // barrier that ends the face phase publishes nxt to the prefetch
     auto find_next = [&]() {
-      if (tid == 0 && next < total_tiles) {
-        lookup(next, nxt);
-        params(nxt, half ^ 1);
-      }
+      if (tid == 0 && next < total_tiles) lookup(next, nxt);
     };
     auto prefetch = [&]() {  // every thread, right after the face phase
       if (next < total_tiles) issue(nxt, dreg);
@@ -148,7 +134,6 @@ __global__ void __launch_bounds__(C::NT, MINB)
       cur[2] = nxt[2];
     }
     first = false;
-    half ^= 1;
   }
 }
 
