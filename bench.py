@@ -354,14 +354,51 @@ def measure_adjoint(E, a, full_tape: bool = True):
             os.environ.pop("E2D_ADJ_FULL_TAPE", None)
         else:
             os.environ["E2D_ADJ_FULL_TAPE"] = old
+    fd = adjoint_fd_check(E, a, p) if full_tape else None
     g, f = min(grads), min(fwd)
     layout = ("every state and its tape kept by the forward sweep, nothing recomputed" if kseg >= ns
               else f"sqrt(N) checkpoints (every {kseg} steps), segments recomputed during the reverse sweep")
     layout += "" if tape else ", reverse steps recomputing their forward values"
-    return {"workload": f"{n}x{n} FP64 HLLC, {ns} steps, dt through the running CFL maximum, {layout}",
+    line = {"workload": f"{n}x{n} FP64 HLLC, {ns} steps, dt through the running CFL maximum, {layout}",
             "segment_steps": kseg, "gradient_ms": round(g, 3), "forward_ms": round(f, 3),
             "adjoint_over_forward": round(g / f, 3),
             "forward_mcells_per_s": round(n * n * ns / (f * 1e-3) / 1e6, 2)}
+    if fd is not None:
+        line["finite_difference_check"] = fd
+    return line
+
+
+def adjoint_fd_check(E, a, p, eps=1e-6, ndir=2):
+    """Central finite differences of J along smooth seeded directions against
+    the adjoint's directional derivative, dt frozen (the logged dt of the
+    gradient).  The state is the implode state with a 1 % smooth density
+    modulation: on the implode state itself the MC limiter (dlft*drgt = 0 on
+    its flat sides) and the CFL maximum (every flat cell ties) are not
+    differentiable."""
+    import numpy as np
+    n, ns = a.adjoint_nx, a.adjoint_steps
+    with E.HydroRun(p, arith=a.arith) as r:
+        r.init_implode()
+        u0 = r.get_state(0)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    u0[0, 2:-2, 2:-2] *= 1.0 + 0.01 * np.sin(2 * np.pi * (X + 0.13)) * np.cos(4 * np.pi * Y + 0.3)
+    rng = np.random.default_rng(4242)
+    errs = []
+    with E.Adjoint(p, arith=a.arith) as A:
+        _, g, dts = A.gradient(ns, u0, dt_mode=0)
+        for _ in range(ndir):
+            d = np.zeros((n, n))
+            for _ in range(4):
+                kx, ky = rng.integers(1, 4, 2)
+                d += rng.normal() * np.sin(np.pi * kx * X + rng.uniform(0, 6)) * np.sin(np.pi * ky * Y + rng.uniform(0, 6))
+            up, um = u0.copy(), u0.copy()
+            up[0, 2:-2, 2:-2] += eps * d
+            um[0, 2:-2, 2:-2] -= eps * d
+            fdv = (A.objective(ns, up, dt_fixed=dts) - A.objective(ns, um, dt_fixed=dts)) / (2 * eps)
+            errs.append(abs(fdv - float(np.sum(g * d))) / abs(fdv))
+    return {"max_rel_err": float(max(errs)), "directions": ndir, "eps": eps, "dt": "frozen",
+            "state": "implode state with a 1 % smooth density modulation (flat states are not differentiable)"}
 
 
 def measure_adjoint_batch(E, a):
