@@ -89,10 +89,11 @@ __global__ void __launch_bounds__(C::NT, MINB)
     if (tid == 0) {
       sh = probs[cur[0]].h;
       *face_counter = 0;
-      const Real dt0 = dt_src ? dt_src[cur[1]] : sh.cfl / *inv_slot<Real>(&ctls[cur[1]], rd);
+      // (the integer-pipe division: the same bits as /, no FP64 pipe work)
+      const Real dt0 = dt_src ? dt_src[cur[1]] : Ops<Real>::div(sh.cfl, *inv_slot<Real>(&ctls[cur[1]], rd));
       sdt[0] = dt0;
-      sdt[1] = dt0 / sh.dx;
-      sdt[2] = dt0 / sh.dy;
+      sdt[1] = Ops<Real>::div(dt0, sh.dx);
+      sdt[2] = Ops<Real>::div(dt0, sh.dy);
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();  // every thread's copies, the problem's parameters and dt

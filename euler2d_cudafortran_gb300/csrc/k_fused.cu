@@ -89,10 +89,10 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     *face_counter = 0;
     // This step's dt (serial_ref/m_run.f90:308 when it comes from the running
     // maximum) and dt/dx, dt/dy (m_run.f90:384-385), once per CTA.
-    const Real dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? h.cfl / *inv_slot<Real>(ctl, sd.rd_slot) : sd.dt_value;
+    const Real dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? Ops<Real>::div(h.cfl, *inv_slot<Real>(ctl, sd.rd_slot)) : sd.dt_value;
     sdt[0] = dt0;
-    sdt[1] = dt0 / h.dx;
-    sdt[2] = dt0 / h.dy;
+    sdt[1] = Ops<Real>::div(dt0, h.dx);  // (the integer-pipe division: the same bits)
+    sdt[2] = Ops<Real>::div(dt0, h.dy);
   }
   __syncthreads();
   if (tid == 0) {
@@ -150,10 +150,10 @@ __global__ void __launch_bounds__(256, E2D_FUSED_MINB64)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     *face_counter = 0;
-    const double dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? h.cfl / *inv_slot<double>(ctl, sd.rd_slot) : sd.dt_value;
+    const double dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? Ops<double>::div(h.cfl, *inv_slot<double>(ctl, sd.rd_slot)) : sd.dt_value;
     sdt[0] = dt0;
-    sdt[1] = dt0 / h.dx;
-    sdt[2] = dt0 / h.dy;
+    sdt[1] = Ops<double>::div(dt0, h.dx);  // (the integer-pipe division: the same bits)
+    sdt[2] = Ops<double>::div(dt0, h.dy);
   }
   __syncthreads();
   if (tid == 0) {
@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *face_counter = 0;
-    const Real dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? h.cfl / *inv_slot<Real>(ctl, sd.rd_slot) : sd.dt_value;
+    const Real dt0 = sd.dt_ptr ? *sd.dt_ptr : sd.from_slot ? Ops<Real>::div(h.cfl, *inv_slot<Real>(ctl, sd.rd_slot)) : sd.dt_value;
     sdt[0] = dt0;
-    sdt[1] = dt0 / h.dx;
-    sdt[2] = dt0 / h.dy;
+    sdt[1] = Ops<Real>::div(dt0, h.dx);  // (the integer-pipe division: the same bits)
+    sdt[2] = Ops<Real>::div(dt0, h.dy);
     if ((int)blockIdx.x < ntiles) issue(blockIdx.x, base + C::q_off);
   }
   __syncthreads();
