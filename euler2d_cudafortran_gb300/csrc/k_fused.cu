@@ -31,7 +31,7 @@ struct FusedPlan {
 
 namespace {
 
-// Tile of the single-run kernel, 256 threads.  FP64: 32 x E2D_FUSED_TY64
+// Tile of the single-run kernel, 256 threads (FP64: E2D_FUSED_NT64).  FP64: 32 x E2D_FUSED_TY64
 // cells at E2D_FUSED_MINB64 CTAs per SM (shared memory and registers must
 // allow that many); FP32: 32 x 15 cells at 4 CTAs per SM (64 registers, 4 x
 // 55 KB of shared memory).  Both need the largest shared-memory carveout.
@@ -41,8 +41,11 @@ namespace {
 #ifndef E2D_FUSED_MINB64
 #define E2D_FUSED_MINB64 2
 #endif
+#ifndef E2D_FUSED_NT64
+#define E2D_FUSED_NT64 256
+#endif
 template <typename Real> struct FusedTile;
-template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, 256>; };
+template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, E2D_FUSED_NT64>; };
 template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 
 #ifndef E2D_PREFETCH_CONS
@@ -64,7 +67,7 @@ __device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* tm, int x, in
 // load is issued (+7 % there; the FP64 step, bound by its FP64 pipe, measured
 // no gain from it).
 template <typename Real, bool SQ, bool QIN>
-__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
+__global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_cons, Hydro<Real> h,
             Field<Real> in, Field<Real> out, Field<Real> qout, StepDt<Real> sd, Ctl* ctl, int fill_ghosts) {
   using C = typename FusedTile<Real>::C;
@@ -131,7 +134,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
 // that also writes its input's primitives, slopes and trace sources to the
 // tape the reverse step reads (tile_compute, TAPE); tape.only: just the tape.
 template <bool SQ>
-__global__ void __launch_bounds__(256, E2D_FUSED_MINB64)
+__global__ void __launch_bounds__(E2D_FUSED_NT64, E2D_FUSED_MINB64)
     k_fused_tape(const __grid_constant__ CUtensorMap tm_in, Hydro<double> h, Field<double> in, Field<double> out,
                  StepDt<double> sd, Ctl* ctl, TapeOut tape) {
   using C = typename FusedTile<double>::C;
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(256, E2D_FUSED_MINB64)
 // With QIN the next box goes straight to the primitives region, which the
 // update phase no longer reads.
 template <typename Real, bool SQ, bool QIN>
-__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
+__global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_cons,
                        Hydro<Real> h, Field<Real> in, Field<Real> out, Field<Real> qout, StepDt<Real> sd, Ctl* ctl,
                        int fill_ghosts, int ntx, int ntiles) {
