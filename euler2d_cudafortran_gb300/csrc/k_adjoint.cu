@@ -421,7 +421,10 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
     sq[k] = (gi < h.isize && gj < h.jsize) ? tape.at(tape.q, v, gj, gi) : 0.0;
     sqb[k] = 0.0;
   }
-  for (int k = tid; k < 12 * NRING; k += ANT) sra[k] = 0.0;
+  // (the source adjoints, planes 8-11, are not accumulated by the faces: a
+  // cell's is half its face states' summed adjoint, which sqb holds; the
+  // ring pass writes those planes before anything reads them)
+  for (int k = tid; k < 8 * NRING; k += ANT) sra[k] = 0.0;
   for (int k = tid; k < 4 * NUB; k += ANT) {
     const int v = k / NUB, rem = k - v * NUB, y = rem / (ATX + 1), x = rem - y * (ATX + 1);
     const int gi = i0 - 1 + x, gj = j0 - 1 + y;
@@ -508,8 +511,6 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
         sqb[v * NBOX + kb] += qrb[v];         // cell b's minus face
         sra[(nrm + v) * NRING + a] += hl;
         sra[(nrm + v) * NRING + b] -= hr;
-        sra[(8 + v) * NRING + a] += hl;
-        sra[(8 + v) * NRING + b] += hr;
       }
     }
     __syncthreads();
@@ -525,6 +526,7 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
     const int x = k % ARX + 1, y = k / ARX + 1;
     const int gi = i0 - GW + x, gj = j0 - GW + y;
     const bool in = gi <= h.nx + 2 && gj <= h.ny + 2;
+    const int kc = y * ABX + x;
     double qc[4], dqx[4], dqy[4], sbar[4], dqxb[4], dqyb[4], qcb[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -533,12 +535,14 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
       dqy[v] = in ? tape.at(tape.dq, 4 + v, gj, gi) : 0.0;
       const double sv = in ? tape.at(tape.s, v, gj, gi) : 0.0;
       dqxb[v] = sra[v * NRING + k]; dqyb[v] = sra[(4 + v) * NRING + k];
-      const double sb = sra[(8 + v) * NRING + k];  // summed per unit dtdx by the face pass
+      // the source adjoint per unit dtdx: half the cell's face-state
+      // adjoints, summed in sqb by the face pass (halving is exact, so this
+      // is bit for bit the sum of the halves)
+      const double sb = Ops<double>::half(sqb[v * NBOX + kc]);
       dts += sv * sb;
       sbar[v] = sb * dtdx;
     }
     adj::trace_sources_rev(h, qc, dqx, dqy, sbar, qcb, dqxb, dqyb);
-    const int kc = y * ABX + x;
     const unsigned cases = (in && lim) ? tape.flag(tape.lim, gj, gi) : 0u;  // the forward's limiter cases
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
