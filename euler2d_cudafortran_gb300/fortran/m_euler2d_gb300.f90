@@ -6,7 +6,8 @@
 !! m_precision / m_constants / m_parameters modules, and instead of m_run.f90):
 !!   gfortran -c m_precision.f90 m_constants.f90 m_parameters.f90 m_monitoring.f90
 !!   gfortran -c m_euler2d_gb300.f90 main.f90
-!!   gfortran -o euler2d *.o -L<path>/_build -leuler2d_gb300 -Wl,-rpath,<path>/_build
+!!   gfortran -o euler2d *.o -L<path>/_build/<machine> -leuler2d_gb300 -Wl,-rpath,<path>/_build/<machine>
+!! (or -leuler2d_gb300_fma, the build with fused multiply-adds)
 !! main.f90 is used unchanged.  No Fortran compiler exists where this project
 !! is built and tested, so this file is shipped uncompiled.
 module m_euler2d_gb300_abi
@@ -28,6 +29,11 @@ module m_euler2d_gb300_abi
        import :: c_int, e2d_params
        type(e2d_params), intent(out) :: p
      end function e2d_default_params
+
+     integer(c_int) function e2d_arithmetic(mode) bind(C, name="e2d_arithmetic")
+       import :: c_int
+       integer(c_int), intent(out) :: mode   ! 0: exact build, 1: fused multiply-adds
+     end function e2d_arithmetic
 
      integer(c_int) function e2d_create(p, h) bind(C, name="e2d_create")
        import :: c_int, c_ptr, e2d_params

@@ -8,7 +8,7 @@ numpy's Fortran front end (f2py's crackfortran):
 
 * every bind(C) interface names a function of include/euler2d_gb300.h, with
   the same number of arguments, scalars passed by value where C takes them
-  by value, pointers as type(c_ptr), value where C takes a pointer, handles
+  by value and by reference where C takes a pointer to one, pointers as type(c_ptr), value where C takes a pointer, handles
   returned through an argument (C: T**) as type(c_ptr) by reference, the
   parameter struct by reference, and an integer(c_int) result;
 * the bind(C) type e2d_params has the C struct's fields, in its order, with
@@ -84,7 +84,8 @@ def test_bind_c_interfaces_match_the_header(modules):
                 assert pointer and "value" not in v.get("attrspec", []), (name, a, cp)
                 assert v.get("typename") == "e2d_params" and "e2d_params" in cp, (name, a, cp)
             else:
-                assert not pointer and "value" in v.get("attrspec", []), (name, a, cp)
+                # a scalar: by value where C takes a value, by reference where C takes a pointer
+                assert pointer == ("value" not in v.get("attrspec", [])), (name, a, cp)
                 kind = v.get("kindselector", {}).get("kind")
                 want = "c_int" if re.match(r"int\b", cp) else "c_double"
                 assert kind == want, (name, a, cp, kind)
