@@ -43,6 +43,7 @@ LIB_NAMES = {"exact": "libeuler2d_gb300.so", "fma": "libeuler2d_gb300_fma.so"}
 LIBS = {k: os.path.join(OUT, v) for k, v in LIB_NAMES.items()}
 LIB = LIBS["exact"]
 EXE = os.path.join(OUT, "euler2d_gb300")
+EXES = {"exact": EXE, "fma": os.path.join(OUT, "euler2d_gb300_fma")}  # the driver linked to each build
 
 CUDA_SOURCES = ["abi.cu", "k_sweeps.cu", "k_fused.cu", "k_probe.cu", "noalloc.cu", "k_selftest.cu", "k_batch.cu",
                 "abi_batch.cu", "k_adjoint.cu", "abi_adjoint.cu", "abi_adjoint_batch.cu"]
@@ -104,10 +105,12 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None,
         if _stale(lib, objs):
             _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs)
     drv = [os.path.join(DRIVER, f) for f in DRIVER_SOURCES]
-    if "exact" in variants and all(os.path.exists(d) for d in drv) and \
-            _stale(EXE, drv + [LIB, os.path.join(DRIVER, "namelist.h")]):
-        _run(["g++", "-O2", "-std=c++17", "-pthread", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-o", EXE]
-             + drv + ["-L", OUT, "-leuler2d_gb300", "-Wl,-rpath,$ORIGIN"])
+    for var in variants:
+        exe, lib = EXES[var], LIBS[var]
+        if all(os.path.exists(d) for d in drv) and _stale(exe, drv + [lib, os.path.join(DRIVER, "namelist.h")]):
+            libname = LIB_NAMES[var][3:-3]  # libX.so -> X
+            _run(["g++", "-O2", "-std=c++17", "-pthread", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+                  "-o", exe] + drv + ["-L", OUT, "-l" + libname, "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

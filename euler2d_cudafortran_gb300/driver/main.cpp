@@ -87,8 +87,11 @@ int main(int argc, char** argv) {
   std::printf(" nStepmax,tEnd,nOutput : %d %g %d\n", cfg.nStepmax, cfg.tEnd, cfg.nOutput);
   std::printf(" gamma0,cfl : %g %g\n smallr,smallc,niter_riemann : %g %g %d\n iorder,slope_type : %d %d\n",
               p.gamma0, p.cfl, p.smallr, p.smallc, p.niter_riemann, p.iorder, p.slope_type);
-  std::printf(" Using implementation version %d, %s Riemann solver, %s\n", p.implementation_version,
-              p.riemann_solver == E2D_RIEMANN_HLLC ? "HLLC" : "approximate", p.precision == 8 ? "FP64" : "FP32");
+  int arith = E2D_ARITH_EXACT;
+  e2d_arithmetic(&arith);
+  std::printf(" Using implementation version %d, %s Riemann solver, %s, %s arithmetic\n", p.implementation_version,
+              p.riemann_solver == E2D_RIEMANN_HLLC ? "HLLC" : "approximate", p.precision == 8 ? "FP64" : "FP32",
+              arith == E2D_ARITH_FMA ? "fused multiply-add" : "exact");
 
   e2d_run* run = nullptr;
   int rc = e2d_create(&p, &run);

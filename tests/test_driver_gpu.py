@@ -92,3 +92,20 @@ def test_begin_download_snapshots_in_stream_order(e2d):
         got = run.wait_download()
         assert np.array_equal(got, ref)
         assert not np.array_equal(run.get_state(0), ref)
+
+
+def test_fma_driver_within_tolerance_of_the_oracle(e2d, oracle, tmp_path):
+    """The same driver linked to the build with fused multiply-adds
+    (-leuler2d_gb300_fma): the same files, the final state within 1e-12
+    relative L1 per variable of the oracle's."""
+    from euler2d_cudafortran_gb300 import build
+    nml = tmp_path / "test.nml"
+    nml.write_text(NML)
+    a = run_driver(build.EXES["fma"], str(nml), str(tmp_path / "fma"))
+    assert len(a) == 6
+    po = oracle.Params(nx=48, ny=40, gamma0=1.4, cfl=0.8, riemann=0, bc_xmin=1, bc_xmax=2, bc_ymin=1, bc_ymax=3)
+    _, _, u, _ = oracle.run(po, 23)
+    got = read_binary_vti(str(tmp_path / "fma" / a[-1]), 48, 40)
+    want = u[:, 2:-2, 2:-2]
+    l1 = [float(np.abs(got[v] - want[v]).sum() / np.abs(want[v]).sum()) for v in range(4)]
+    assert max(l1) <= 1e-12, l1
