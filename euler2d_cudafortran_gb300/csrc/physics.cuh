@@ -547,19 +547,19 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   Real ro, uo, ptoto, etoto;
 #if E2D_FMA_FORMS
   // the star states reuse rcl = rl (ul - SL) and rcr = rr (SR - ur):
-  // rl (SL - ul) / (SL - ustar) = rcl / (ustar - SL), and so on
+  // rl (SL - ul) / (SL - ustar) = rcl / (ustar - SL), and so on.  One star
+  // state, its side chosen by selects: a warp whose faces sample both star
+  // states issues it once.
   if (O::gt0(SL)) {
     ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
-  } else if (O::gt0(ustar)) {
-    const Real d = ustar - SL;
-    ro = O::div(rcl, d);
+  } else if (O::gt0(ustar) || O::gt0(SR)) {
+    const bool lk = O::gt0(ustar);  // the left star state
+    const Real ps = ptotstar * ustar;
+    const Real d = lk ? ustar - SL : SR - ustar;
+    ro = O::div(lk ? rcl : rcr, d);
     uo = ustar; ptoto = ptotstar;
-    etoto = O::div(fmx(ul - SL, etotl, fmx(ptotl, ul, -(ptotstar * ustar))), d);
-  } else if (O::gt0(SR)) {
-    const Real d = SR - ustar;
-    ro = O::div(rcr, d);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div(fmx(SR - ur, etotr, fmx(-ptotr, ur, ptotstar * ustar)), d);
+    etoto = O::div(fmx(lk ? ul - SL : SR - ur, lk ? etotl : etotr,
+                       fmx(O::neg_if(lk ? ptotl : ptotr, !lk), lk ? ul : ur, O::neg_if(ps, lk))), d);
   } else {
     ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
   }
