@@ -105,3 +105,31 @@ def test_batch_tape_gives_the_recomputed_gradient(e2d, monkeypatch):
         assert abs(J1[k] - J2[k]) <= 1e-13 * abs(J2[k])
         assert np.any(g1[k] != 0.0)
         assert rel_l1(g1[k], g2[k]) <= 1e-12, (k, rel_l1(g1[k], g2[k]))
+
+
+@pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
+def test_fma_batch_adjoint_equals_single_problem_adjoints(e2d, oracle, dt_mode):
+    """The build with fused multiply-adds: each problem's gradient from the
+    batch equals its single-problem adjoint's (to round-off) on states
+    modulated by 1 % random noise (no ties for the two paths' roundings to
+    break differently)."""
+    n = 23
+    rng = np.random.default_rng(31)
+    states = []
+    for k in range(len(SIZES)):
+        _, po, u0 = single_params(e2d, oracle, k)
+        u0 = u0.copy()
+        u0[0, 2:-2, 2:-2] *= 1.0 + 0.01 * rng.standard_normal((po.ny, po.nx))
+        states.append(u0)
+    with e2d.AdjointBatch(SIZES, BCS, gamma0=1.4, cfl=0.8, arith="fma") as b:
+        for k, u0 in enumerate(states):
+            b.set_state(k, u0)
+        J, grads, dts = b.gradient(n, dt_mode=dt_mode)
+    for k in range(len(SIZES)):
+        pe, _, _ = single_params(e2d, oracle, k)
+        with e2d.Adjoint(pe, arith="fma") as A:
+            Js, gs, dts_s = A.gradient(n, states[k], dt_mode=dt_mode)
+        assert float(np.max(np.abs(dts[:, k] - dts_s) / dts_s)) <= 1e-14, f"problem {k}: dt sequence"
+        assert abs(J[k] - Js) <= 1e-12 * abs(Js), (k, J[k], Js)
+        assert rel_l1(grads[k], gs) <= 1e-9, (k, rel_l1(grads[k], gs))
+        assert np.any(grads[k] != 0.0)

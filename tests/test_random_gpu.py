@@ -107,3 +107,22 @@ def test_random_configuration_fma_build(e2d, oracle, k):
             l1 = _rel_l1(gpu, ref, c["gamma0"])
             dr = float(np.max(np.abs(dts.astype(np.float64) - dts_ref) / np.abs(dts_ref)))
             assert max(l1) <= l1_tol and dr <= dt_tol, (c, version, prec, l1, dr)
+
+
+@pytest.mark.parametrize("k", range(len(ADJ)))
+@pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
+def test_random_adjoint_fma_build_matches_tangent(e2d, oracle, k, dt_mode):
+    """The adjoint of the build with fused multiply-adds on the same random
+    configurations (density modulated by 1 % random noise: no ties for the
+    two arithmetics to break differently) against the oracle's tangent, to
+    1e-7 relative."""
+    c = dict(ADJ[k], riemann=2)
+    pe, po = _params(e2d, oracle, c, 0)
+    u0 = oracle.init_diagonal(po, c["offset"], c["rho_hi"], c["p_hi"], c["rho_lo"], c["p_lo"])
+    u0[0, 2:-2, 2:-2] *= 1.0 + 0.01 * np.random.default_rng(k).standard_normal((c["ny"], c["nx"]))
+    with e2d.Adjoint(pe, arith="fma") as A:
+        J, g, dts = A.gradient(c["nsteps"], u0, dt_mode=dt_mode)
+    d = np.random.default_rng(100 + k).normal(size=(c["ny"], c["nx"]))
+    Jt, dJt = oracle.tangent(po, u0, d, c["nsteps"], nthreads=NTHREADS, fixed_dts=dts if dt_mode == 0 else None)
+    assert abs(J - Jt) <= 1e-12 * abs(Jt)
+    assert abs(float(np.sum(g * d)) - dJt) <= 1e-7 * abs(dJt), (c, float(np.sum(g * d)), dJt)
