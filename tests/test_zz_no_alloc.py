@@ -31,14 +31,15 @@ def _rel_l1(a, b):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("arith", ["exact", "fma"])
 @pytest.mark.parametrize("precision", [8, 4])
-def test_noalloc_step_matches_regular_step_two_calls(e2d, precision):
+def test_noalloc_step_matches_regular_step_two_calls(e2d, precision, arith):
     torch = pytest.importorskip("torch")
     p = e2d.make_params(nx=96, ny=80, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
                         implementation_version=0, precision=precision)
-    lib = e2d.load_library()
+    lib = e2d.load_library(arith)
     stream = torch.cuda.Stream()
-    with e2d.HydroRun(p) as ref, e2d.HydroRun(p) as buf:
+    with e2d.HydroRun(p, arith=arith) as ref, e2d.HydroRun(p, arith=arith) as buf:
         # the existing entry point, called as serial_ref/main.f90 calls it
         ref.init_implode()
         ref.compute_dt(0)
@@ -64,10 +65,14 @@ def test_noalloc_step_matches_regular_step_two_calls(e2d, precision):
         assert rc == 0, lib.e2d_last_error().decode()
         got2 = buf.get_state(0)
 
-    assert _rel_l1(got1, want1) <= REL_L1_TOL
-    assert _rel_l1(got2, want2) <= REL_L1_TOL
-    assert np.array_equal(_interior(got1), _interior(want1))
-    assert np.array_equal(_interior(got2), _interior(want2))
+    # the exact build: bitwise; the FMA build's two paths (fused step, stored
+    # fluxes) round differently: the FP64 bar of the other tests, and 1e-5 in FP32
+    tol = REL_L1_TOL if (arith == "exact" or precision == 8) else 1e-5
+    assert _rel_l1(got1, want1) <= tol
+    assert _rel_l1(got2, want2) <= tol
+    if arith == "exact":
+        assert np.array_equal(_interior(got1), _interior(want1))
+        assert np.array_equal(_interior(got2), _interior(want2))
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(e2d):
