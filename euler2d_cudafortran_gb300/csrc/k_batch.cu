@@ -16,6 +16,10 @@
 
 namespace e2d {
 
+#ifndef E2D_BATCH_CARRY
+#define E2D_BATCH_CARRY 1
+#endif
+
 namespace {
 
 // 16-byte asynchronous copy global -> shared; the bytes past src_bytes (0, 8
@@ -27,10 +31,15 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int sr
 // SQ: every problem of the launch has dx == dy (the shared face source term
 // of tile_compute).  QIN: the boxes are read from the primitives kept beside
 // the states, and the update writes those of the new state (tile_compute).
-// A CTA walks the flattened tiles with a fixed stride; the box of its next
-// tile is copied asynchronously (cp.async) as soon as the face phase of the
-// current one ends -- into the primitives region with QIN, else into the
-// slope region -- so it lands while the update phase runs.
+// A CTA walks one contiguous run of the flattened tiles (runs differ by at
+// most one tile); within a problem the tiles are listed column by column, so
+// that consecutive tiles of a run are mostly a tile and the one above it,
+// which takes over the lower tile's top ring rows and y-face row
+// (tile_compute's carry).  The box of the CTA's next tile is copied asynchronously
+// (cp.async) into the box region as soon as the face phase of the current one
+// ends (no later phase reads the box), so it lands while the update phase
+// runs.  A problem's parameters and dt are loaded when the run enters it, not
+// per tile.
 // TAPE (FP64, !QIN): the step also writes each problem's tape (BatchProb::tape).
 template <typename Real, class C, int MINB, bool SQ, bool QIN, bool TAPE = false>
 __global__ void __launch_bounds__(C::NT, MINB)
@@ -45,9 +54,8 @@ __global__ void __launch_bounds__(C::NT, MINB)
   __shared__ Hydro<Real> sh;
   __shared__ int cur[3], nxt[3];  // problem (work-list order), problem index, tile within the problem
   const int tid = threadIdx.x;
-  Real* const dreg = QIN ? base + C::q_off : base + C::d_off;  // where a prefetched box lands
-  static_assert(8ull * C::RY * C::RX >= 4ull * C::BYs * C::BXs, "the next box fits in the slope region");
-  static_assert((C::d_off * sizeof(Real)) % 16 == 0 && (C::BXs * sizeof(Real)) % 16 == 0,
+  Real* const dreg = base + C::q_off;  // where a prefetched box lands (read by no phase after the faces)
+  static_assert((C::q_off * sizeof(Real)) % 16 == 0 && (C::BXs * sizeof(Real)) % 16 == 0,
                 "16-byte aligned copy destinations");
 
   auto lookup = [&](int t, int* info) {  // thread 0
@@ -63,7 +71,7 @@ __global__ void __launch_bounds__(C::NT, MINB)
   };
   auto issue = [&](const int* info, Real* dst) {  // every thread: its part of the box of tile `info`
     const BatchProb<Real>& P = probs[info[0]];
-    const int i0 = GW + (info[2] % P.ntx) * C::TX, j0 = GW + (info[2] / P.ntx) * C::TY;
+    const int i0 = GW + (info[2] / P.nty) * C::TX, j0 = GW + (info[2] % P.nty) * C::TY;
     const Real* b = QIN ? (parity ? P.q2 : P.q) : (parity ? P.u2 : P.u);
     const int isize = P.h.isize, jsize = P.h.jsize;
     constexpr int CH = 16 / (int)sizeof(Real), NCH = C::BXs / CH;
@@ -79,16 +87,22 @@ __global__ void __launch_bounds__(C::NT, MINB)
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
 
-  int t = blockIdx.x;
-  if (t >= total_tiles) return;
-  if (tid == 0) lookup(t, cur);
+  // this CTA's run of the work list: [t_begin, t_end)
+  const int per = total_tiles / (int)gridDim.x, extra = total_tiles % (int)gridDim.x, bid = (int)blockIdx.x;
+  const int t_begin = bid * per + min(bid, extra), t_end = t_begin + per + (bid < extra ? 1 : 0);
+  if (t_begin >= t_end) return;
+  if (tid == 0) {
+    lookup(t_begin, cur);
+    *face_counter = 0;
+  }
   __syncthreads();
   issue(cur, base + C::q_off);
   bool first = true;
-  for (; t < total_tiles; t += gridDim.x) {
-    if (tid == 0) {
-      sh = probs[cur[0]].h;
-      *face_counter = 0;
+  int loaded = -1;  // the work-list problem whose parameters and dt are in sh / sdt
+  for (int t = t_begin; t < t_end; ++t) {
+    if (tid == 0 && cur[0] != loaded) {
+      loaded = cur[0];
+      sh = probs[loaded].h;
       // (the integer-pipe division: the same bits as /, no FP64 pipe work)
       const Real dt0 = dt_src ? dt_src[cur[1]] : Ops<Real>::div(sh.cfl, *inv_slot<Real>(&ctls[cur[1]], rd));
       sdt[0] = dt0;
@@ -99,24 +113,36 @@ __global__ void __launch_bounds__(C::NT, MINB)
     __syncthreads();  // every thread's copies, the problem's parameters and dt
     const int p = cur[0], id = cur[1], stile = cur[2];
     const BatchProb<Real>& P = probs[p];
-    const int i0 = GW + (stile % P.ntx) * C::TX, j0 = GW + (stile / P.ntx) * C::TY;
+    const int i0 = GW + (stile / P.nty) * C::TX, j0 = GW + (stile % P.nty) * C::TY;
     Field<Real> in{parity ? P.u2 : P.u, P.pitch, P.plane};
     Field<Real> out{parity ? P.u : P.u2, P.pitch, P.plane};
     const Field<Real> qout{QIN ? (parity ? P.q : P.q2) : out.p, P.pitch, P.plane};
-    const int next = t + gridDim.x;
-    // thread 0 finds the next tile's problem at the start of the face phase,
-    // where warps claim faces dynamically and no barrier waits for it; the
+    const int next = t + 1;
+    const int ptiles = P.ntx * P.nty;
+    // thread 0 names the next tile (this problem's next one, or the first of
+    // the next problem in the work list) at the start of the face phase; the
     // barrier that ends the face phase publishes nxt to the prefetch
     auto find_next = [&]() {
-      if (tid == 0 && next < total_tiles) lookup(next, nxt);
+      if (tid == 0 && next < t_end) {
+        const bool same = stile + 1 < ptiles;
+        nxt[0] = same ? p : p + 1;
+        nxt[1] = same ? id : probs[p + 1].id;
+        nxt[2] = same ? stile + 1 : 0;
+      }
     };
     auto prefetch = [&]() {  // every thread, right after the face phase
-      if (next < total_tiles) issue(nxt, dreg);
+      if (next < t_end) issue(nxt, dreg);
     };
+    // the tile below was this CTA's previous one / the next one is the tile above
+    const int carry = E2D_BATCH_CARRY
+                          ? ((!first && stile % P.nty != 0) ? kCarryIn : 0) |
+                                ((next < t_end && stile + 1 < ptiles && (stile + 1) % P.nty != 0) ? kCarryOut : 0)
+                          : 0;
     const bool only = TAPE && P.tape.only;  // a tape-only pass: no update, no dt
     Real m = tile_compute<Real, C, SQ, QIN, TAPE>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1],
                                                   sdt[2], true, wr >= 0 && !only, &ctls[id].health,
-                                                  (QIN || first) ? nullptr : dreg, prefetch, &P.tape, find_next);
+                                                  nullptr, prefetch, &P.tape, find_next,
+                                                  carry);
     if (tid == 0 && !only) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];
@@ -128,12 +154,13 @@ __global__ void __launch_bounds__(C::NT, MINB)
         atomic_max_slot_ptr<Real>(inv_slot<Real>(&ctls[id], wr), m);
       }
     }
-    __syncthreads();  // the tile's shared data consumed
     if (tid == 0) {
+      *face_counter = 0;
       cur[0] = nxt[0];
       cur[1] = nxt[1];
       cur[2] = nxt[2];
     }
+    __syncthreads();  // the tile's shared data consumed; the next tile named
     first = false;
   }
 }

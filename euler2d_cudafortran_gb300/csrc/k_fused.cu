@@ -51,6 +51,9 @@ template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 #ifndef E2D_PREFETCH_CONS
 #define E2D_PREFETCH_CONS 1
 #endif
+#ifndef E2D_PREFETCH_CONS64
+#define E2D_PREFETCH_CONS64 1
+#endif
 
 // Asks the TMA unit to bring a box of the map into L2 (no completion to wait for).
 __device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* tm, int x, int y) {
@@ -62,10 +65,10 @@ __device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* tm, int x, in
 
 // SQ: dx == dy (the shared face source term of tile_compute).  QIN: tm_in
 // maps the primitives of the input state, and the primitives of the output
-// go to qout (tile_compute); in FP32 the tile's conservative values, which
-// only the update reads, are prefetched into L2 through tm_cons when the box
-// load is issued (+7 % there; the FP64 step, bound by its FP64 pipe, measured
-// no gain from it).
+// go to qout (tile_compute); the tile's conservative values, which only the
+// update reads, are prefetched into L2 through tm_cons when the box load is
+// issued (FP32: +7 %; the FP64 persistent kernel, whose column-ordered walk
+// finds fewer of them in L2: +0.9 %).
 template <typename Real, bool SQ, bool QIN>
 __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_cons, Hydro<Real> h,
@@ -194,26 +197,47 @@ __global__ void __launch_bounds__(E2D_FUSED_NT64, E2D_FUSED_MINB64)
 #ifndef E2D_FUSED_PERSISTENT
 #define E2D_FUSED_PERSISTENT 1
 #endif
+// The taping step walks the tiles as the persistent step does (carry
+// included); E2D_TAPE_PERSISTENT=0 launches one CTA per tile (k_fused_tape).
+#ifndef E2D_TAPE_PERSISTENT
+#define E2D_TAPE_PERSISTENT 1
+#endif
+// FP32 may take the persistent kernel too when its box is primitives (QIN:
+// the next box lands in the 128-byte aligned primitives region); off, as
+// measured: 19.4 against 19.7 Gcell/s for one CTA per tile at 2048^2.
+#ifndef E2D_FUSED_PERSISTENT32
+#define E2D_FUSED_PERSISTENT32 0
+#endif
+template <typename Real, bool QIN>
+constexpr bool use_persistent() {
+  return sizeof(Real) == 8 ? E2D_FUSED_PERSISTENT != 0 : (E2D_FUSED_PERSISTENT32 != 0 && QIN);
+}
 #ifndef E2D_SQ_TRACE
 #define E2D_SQ_TRACE 1
 #endif
 
 // Persistent variant (FP64, the default; E2D_FUSED_PERSISTENT=0 selects one
-// CTA per tile): a grid of resident CTAs walks the tiles with a fixed stride.  The box of a CTA's next tile is loaded by TMA into the slope
-// region as soon as the face phase of the current tile has ended (the slopes
-// and sources are no longer read then), so the load lands while the update
-// phase runs; the primitives phase of the next tile reads it from there.
-// One mbarrier, one phase per load; every wait is bounded.
-// With QIN the next box goes straight to the primitives region, which the
-// update phase no longer reads.
-template <typename Real, bool SQ, bool QIN>
+// CTA per tile): a grid of resident CTAs, each walking one contiguous run of
+// the tiles in column order (up a column of tiles, then on to the next
+// column; runs differ by at most one tile).  The box of a CTA's next tile is
+// loaded by TMA into the box region as soon as the face phase of the current
+// tile has ended (no later phase reads the box), so the load lands while the
+// update phase runs.  One mbarrier, one phase per load; every wait is
+// bounded.  A tile directly above the previous one takes over its top two
+// ring rows and top y-face row (tile_compute's carry: 12 % fewer ring cells
+// and 6 % fewer y faces at 32 x 15).
+// TAPE (FP64, conservative boxes): the adjoint's forward step that also
+// writes its input's forward values to `tape` (tape.only: just the tape).
+#ifndef E2D_CARRY
+#define E2D_CARRY 1
+#endif
+template <typename Real, bool SQ, bool QIN, bool TAPE = false>
 __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, sizeof(Real) == 8 ? E2D_FUSED_MINB64 : 4)
     k_fused_persistent(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_cons,
                        Hydro<Real> h, Field<Real> in, Field<Real> out, Field<Real> qout, StepDt<Real> sd, Ctl* ctl,
-                       int fill_ghosts, int ntx, int ntiles) {
+                       int fill_ghosts, int nty, int ntiles, TapeOut tape) {
+  static_assert(!TAPE || (sizeof(Real) == 8 && !QIN), "the tape is written by the FP64 conversion path");
   using C = typename FusedTile<Real>::C;
-  static_assert(8ull * C::RY * C::RX >= 4ull * C::BYs * C::BXs, "the next box fits in the slope region");
-  static_assert((C::d_off * sizeof(Real)) % 128 == 0, "TMA destination alignment of the slope region");
   extern __shared__ unsigned char smem_raw[];
   Real* base = reinterpret_cast<Real*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   unsigned char* tail = reinterpret_cast<unsigned char*>(base + C::n_real);
@@ -221,11 +245,14 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
   int* face_counter = reinterpret_cast<int*>(tail + 8);
   Real* red = reinterpret_cast<Real*>(tail + 16);
   Real* sdt = red + 32;
-  Real* dreg = QIN ? base + C::q_off : base + C::d_off;
+  Real* const dreg = base + C::q_off;  // where the next box lands (read by no phase after the faces)
   const int tid = threadIdx.x;
   const uint32_t bar_a = smem_u32(bar);
+  // this CTA's run of tiles [t_begin, t_end); tile t is column t / nty, row t % nty
+  const int per = ntiles / (int)gridDim.x, extra = ntiles % (int)gridDim.x, b = (int)blockIdx.x;
+  const int t_begin = b * per + min(b, extra), t_end = t_begin + per + (b < extra ? 1 : 0);
   auto issue = [&](int t, Real* dst) {  // thread 0: the box of tile t into dst
-    const int i0 = GW + (t % ntx) * C::TX, j0 = GW + (t / ntx) * C::TY;
+    const int i0 = GW + (t / nty) * C::TX, j0 = GW + (t % nty) * C::TY;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(C::box_bytes)
                  : "memory");
@@ -234,7 +261,7 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
             "r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
         : "memory");
-    if (QIN && E2D_PREFETCH_CONS && sizeof(Real) == 4) prefetch_box_l2(&tm_cons, i0 - GW, j0 - GW);
+    if (QIN && E2D_PREFETCH_CONS && (sizeof(Real) == 4 || E2D_PREFETCH_CONS64)) prefetch_box_l2(&tm_cons, i0 - GW, j0 - GW);
   };
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
@@ -244,28 +271,34 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
     sdt[0] = dt0;
     sdt[1] = Ops<Real>::div(dt0, h.dx);  // (the integer-pipe division: the same bits)
     sdt[2] = Ops<Real>::div(dt0, h.dy);
-    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, base + C::q_off);
+    if (t_begin < t_end) issue(t_begin, base + C::q_off);
   }
   __syncthreads();
-  const bool want_dt = sd.wr_slot >= 0;
+  const bool only = TAPE && tape.only;  // a tape-only pass: no update, no dt
+  const bool want_dt = sd.wr_slot >= 0 && !only;
   Real mmax = Real(0);
   uint32_t parity = 0;
   bool first = true;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  for (int t = t_begin; t < t_end; ++t) {
     const bool ok = mbar_wait(bar_a, parity, kTmaWaitCycles);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(&ctl->health, 4u);
       return;
     }
     parity ^= 1;
-    const int next = t + gridDim.x;
-    const int i0 = GW + (t % ntx) * C::TX, j0 = GW + (t / ntx) * C::TY;
+    const int next = t + 1;
+    const int i0 = GW + (t / nty) * C::TX, j0 = GW + (t % nty) * C::TY;
     auto prefetch = [&]() {
-      if (tid == 0 && next < ntiles) issue(next, dreg);
+      if (tid == 0 && next < t_end) issue(next, dreg);
     };
-    const Real m = tile_compute<Real, C, SQ, QIN>(h, base, face_counter, red, i0, j0, in, out, qout, sdt[1],
-                                                  sdt[2], fill_ghosts != 0, want_dt, &ctl->health,
-                                                  (QIN || first) ? nullptr : dreg, prefetch);
+    // the tile below was this CTA's previous one / the next one is the tile above
+    const int carry = E2D_CARRY
+                          ? ((!first && t % nty != 0) ? kCarryIn : 0) | ((next < t_end && next % nty != 0) ? kCarryOut : 0)
+                          : 0;
+    const Real m = tile_compute<Real, C, SQ, QIN, TAPE>(h, base, face_counter, red, i0, j0, in, out, qout,
+                                                        sdt[1], sdt[2], fill_ghosts != 0, want_dt, &ctl->health,
+                                                        nullptr, prefetch, TAPE ? &tape : nullptr, NoHook(),
+                                                        carry);
     if (tid == 0) {
       mmax = Ops<Real>::max(mmax, m);
       *face_counter = 0;
@@ -273,7 +306,7 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
     __syncthreads();  // this tile's shared data consumed; the counter reset is visible
     first = false;
   }
-  if (tid == 0) {
+  if (tid == 0 && !only) {
     const Real dt = sdt[0];
     if (blockIdx.x == 0) {
       if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
@@ -292,7 +325,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 // Resident CTAs per SM x SMs of the current device (the persistent grid).
-template <typename Real, bool SQ, bool QIN>
+template <typename Real, bool SQ, bool QIN, bool TAPE = false>
 int persistent_grid() {
   static int grid[64] = {0};
   int dev = 0;
@@ -302,7 +335,8 @@ int persistent_grid() {
     using C = typename FusedTile<Real>::C;
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real, SQ, QIN>, C::NT, C::bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_persistent<Real, SQ, QIN, TAPE>, C::NT,
+                                                  C::bytes);
     grid[dev] = std::max(1, sms * std::max(1, per_sm));
   }
   return grid[dev];
@@ -310,6 +344,16 @@ int persistent_grid() {
 
 // Dynamic shared memory of the tile, and the largest shared-memory carveout
 // so that as many CTAs as the launch bounds ask for fit on an SM.
+template <typename Real, bool SQ, bool QIN, bool TAPE = false>
+bool set_persistent_attributes() {
+  using C = typename FusedTile<Real>::C;
+  return cudaFuncSetAttribute(k_fused_persistent<Real, SQ, QIN, TAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)C::bytes) == cudaSuccess &&
+         cudaFuncSetAttribute(k_fused_persistent<Real, SQ, QIN, TAPE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
+         persistent_grid<Real, SQ, QIN, TAPE>() > 0;  // sized here, outside any stream capture
+}
+
 template <typename Real, bool SQ, bool QIN>
 bool set_fused_attributes_sq() {
   using C = typename FusedTile<Real>::C;
@@ -317,13 +361,7 @@ bool set_fused_attributes_sq() {
                                  (int)C::bytes) == cudaSuccess &&
             cudaFuncSetAttribute(k_fused<Real, SQ, QIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
-  if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT)
-    ok = ok &&
-         cudaFuncSetAttribute(k_fused_persistent<Real, SQ, QIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)C::bytes) == cudaSuccess &&
-         cudaFuncSetAttribute(k_fused_persistent<Real, SQ, QIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                              (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
-         persistent_grid<Real, SQ, QIN>() > 0;  // sized here, outside any stream capture
+  if constexpr (use_persistent<Real, QIN>()) ok = ok && set_persistent_attributes<Real, SQ, QIN>();
   return ok;
 }
 
@@ -342,6 +380,9 @@ bool set_fused_attributes() {
                               (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess &&
          cudaFuncSetAttribute(k_fused_tape<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
                               (int)cudaSharedmemCarveoutMaxShared) == cudaSuccess;
+    if constexpr (E2D_FUSED_PERSISTENT && E2D_TAPE_PERSISTENT)
+      ok = ok && set_persistent_attributes<double, false, false, true>() &&
+           set_persistent_attributes<double, true, false, true>();
   }
   return ok;
 }
@@ -352,10 +393,11 @@ void launch_fused_sq(const CUtensorMap& tm, const CUtensorMap& tmc, const Hydro<
                      cudaStream_t s) {
   using C = typename FusedTile<Real>::C;
   const int ntx = (h.nx + C::TX - 1) / C::TX, nty = (h.ny + C::TY - 1) / C::TY;
-  if constexpr (sizeof(Real) == 8 && E2D_FUSED_PERSISTENT) {
+  if constexpr (use_persistent<Real, QIN>()) {
     const int grid = std::min(ntx * nty, persistent_grid<Real, SQ, QIN>());
     k_fused_persistent<Real, SQ, QIN><<<grid, C::NT, C::bytes, s>>>(tm, tmc, h, in, out, qout, sd, ctl,
-                                                                    fill_ghosts ? 1 : 0, ntx, ntx * nty);
+                                                                    fill_ghosts ? 1 : 0, nty, ntx * nty,
+                                                                    TapeOut{});
   } else {
     k_fused<Real, SQ, QIN><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, tmc, h, in, out, qout, sd, ctl,
                                                                    fill_ghosts ? 1 : 0);
@@ -468,13 +510,25 @@ void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in,
   launch_fused_tm<Real>(tm, tm, h, in, out, nullptr, sd, ctl, fill_ghosts, s);
 }
 
+template <bool SQ>
+void launch_fused_tape_sq(const CUtensorMap& tm, const Hydro<double>& h, Field<double> in, Field<double> out,
+                          StepDt<double> sd, Ctl* ctl, const TapeOut& tape, cudaStream_t s) {
+  using C = typename FusedTile<double>::C;
+  const int ntx = (h.nx + C::TX - 1) / C::TX, nty = (h.ny + C::TY - 1) / C::TY;
+  if constexpr (E2D_FUSED_PERSISTENT && E2D_TAPE_PERSISTENT) {
+    const int grid = std::min(ntx * nty, persistent_grid<double, SQ, false, true>());
+    k_fused_persistent<double, SQ, false, true><<<grid, C::NT, C::bytes, s>>>(tm, tm, h, in, out, out, sd, ctl, 1,
+                                                                              nty, ntx * nty, tape);
+  } else {
+    k_fused_tape<SQ><<<dim3(ntx, nty), C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, tape);
+  }
+}
+
 void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double> in, Field<double> out,
                        StepDt<double> sd, Ctl* ctl, const TapeOut& tape, cudaStream_t s) {
-  using C = typename FusedTile<double>::C;
   const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(map.bytes);
-  const dim3 grid((h.nx + C::TX - 1) / C::TX, (h.ny + C::TY - 1) / C::TY);
-  if (E2D_SQ_TRACE && h.dx == h.dy) k_fused_tape<true><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, tape);
-  else k_fused_tape<false><<<grid, C::NT, C::bytes, s>>>(tm, h, in, out, sd, ctl, tape);
+  if (E2D_SQ_TRACE && h.dx == h.dy) launch_fused_tape_sq<true>(tm, h, in, out, sd, ctl, tape, s);
+  else launch_fused_tape_sq<false>(tm, h, in, out, sd, ctl, tape, s);
 }
 
 void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, Field<double> in, Field<double> out,

@@ -87,6 +87,18 @@ __device__ __forceinline__ bool owns(int g, int t0, int w, int n) {
 // before_faces: run by every thread right after the barrier that ends the
 // ring pass, before it claims faces (work there delays no barrier: the faces
 // are claimed dynamically).
+// carry (a CTA that walks a column of tiles upwards):
+//   kCarryIn: the previous call of this CTA computed the tile below (j0 - TY)
+//     and kCarryOut; its top two ring rows (slopes and face sources of the
+//     tile rows -1 and 0 of this one) then sit in ring rows 0-1, and its top
+//     y-face row (the faces below this tile's row 0) in sfy row TY.  Those
+//     are not computed again: the same inputs and the same code give the
+//     same bits.
+//   kCarryOut: the next call computes the tile above with kCarryIn: after
+//     the face phase, ring rows RY-2..RY-1 are copied to rows 0-1.  With
+//     TAPE this call also records the ring row and y-face row that the tile
+//     above owns but does not compute.
+constexpr int kCarryIn = 1, kCarryOut = 2;
 template <typename Real, class C, bool SQ = false, bool QIN = false, bool TAPE = false, class Hook = NoHook,
           class Hook2 = NoHook>
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
@@ -94,9 +106,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
                                              const Field<Real>& qout, Real dtdx, Real dtdy, bool fill_ghosts,
                                              bool want_dt, unsigned* health, const Real* box_src = nullptr,
                                              Hook after_faces = Hook(), const TapeOut* tape = nullptr,
-                                             Hook2 before_faces = Hook2()) {
+                                             Hook2 before_faces = Hook2(), int carry = 0) {
   static_assert(!TAPE || (sizeof(Real) == 8 && !QIN), "the tape is written by the FP64 conversion path");
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, BXs = C::BXs, BYs = C::BYs, RX = C::RX, RY = C::RY;
+  static_assert(RY >= 4 && TX % 32 == 0, "carried ring rows do not overlap their copies; whole y-face chunks");
   Real* sq = base + C::q_off;
   Real* sdq = base + C::d_off;
   Real* ss = base + C::s_off;
@@ -131,12 +144,23 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
 
   // ---- slopes and trace source terms of the ring cells (-1..TX, -1..TY)
   auto Q = [&](int v, int y, int x) -> Real { return sq[(v * BYs + y) * BXs + x]; };
+  // carried in: the y-face row below tile row 0 is the previous tile's top
+  // row (its update has read it: the caller's barrier ends that tile)
+  const bool carried = (carry & kCarryIn) != 0;
+  if (carried) {
+    for (int k = tid; k < 4 * TX; k += NT) {
+      const int v = k / TX, c = k % TX;
+      sfy[(v * (TY + 1)) * TX + c] = sfy[(v * (TY + 1) + TY) * TX + c];
+    }
+  }
   // ring cells in warp-aligned rows: the first TX columns of every row, then
-  // the last RX - TX columns (a warp then reads one row of consecutive words)
+  // the last RX - TX columns (a warp then reads one row of consecutive words);
+  // rows 0-1 are skipped when carried in
   static_assert(RX - TX == 2, "the ring is two columns wider than the tile");
-  for (int k = tid; k < RX * RY; k += NT) {
-    const int x = k < TX * RY ? k % TX + 1 : TX + 1 + (k - TX * RY) % 2;  // box coordinates
-    const int y = k < TX * RY ? k / TX + 1 : (k - TX * RY) / 2 + 1;
+  const int ys = carried ? 2 : 0, rows = RY - ys;
+  for (int k = tid; k < RX * rows; k += NT) {
+    const int x = k < TX * rows ? k % TX + 1 : TX + 1 + (k - TX * rows) % 2;  // box coordinates
+    const int y = (k < TX * rows ? k / TX : (k - TX * rows) / 2) + 1 + ys;
     const int kr = (y - 1) * RX + (x - 1);                                 // ring index
     Real qc[4], qe[4], qw[4], qn[4], qs[4], dqx[4], dqy[4], s[4];
 #pragma unroll
@@ -155,7 +179,10 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
 #endif
     if constexpr (TAPE) {
       const int gi = i0 - GW + x, gj = j0 - GW + y;
-      if (gi <= h.nx + 2 && gj <= h.ny + 2 && owns(gi, i0, TX, h.nx) && owns(gj, j0, TY, h.ny)) {
+      // (with kCarryOut also the top ring row, which the tile above owns but
+      // takes over instead of computing)
+      if (gi <= h.nx + 2 && gj <= h.ny + 2 && owns(gi, i0, TX, h.nx) &&
+          (owns(gj, j0, TY, h.ny) || ((carry & kCarryOut) && y == RY && owns(gj, j0 + TY, TY, h.ny)))) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           tape->at(tape->dq, v, gj, gi) = dqx[v];
@@ -190,7 +217,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   // (every FP64 instruction a warp issues costs its FP64 pipe slots,
   // predicated or not).
   constexpr int NXF = (TX + 1) * TY, NYF = TX * (TY + 1);
-  constexpr int Y0 = (NXF + 31) / 32 * 32, NF = Y0 + NYF;
+  constexpr int Y0 = (NXF + 31) / 32 * 32;
+  // carried in: y-face row 0 is not solved again (a whole number of chunks)
+  const int yskip = carried ? TX : 0, NF = Y0 + NYF - yskip;
   const int lane = tid & 31;
   before_faces();
   while (true) {
@@ -244,7 +273,7 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
         for (int v = 0; v < 4; ++v) sfx[(v * TY + r) * (TX + 1) + f] = kFluxRaw ? flux[v] : flux[v] * dtdx;
       }
     } else if (k >= Y0 && k < NF) {
-      const int kk = k - Y0;
+      const int kk = k - Y0 + yskip;
       const int c = kk % TX, g = kk / TX;  // between ring cells (c, g-1) and (c, g)
       if (i0 + c <= h.nx + 1 && j0 + g <= h.ny + 2) {
         const int kl = g * RX + (c + 1), kr = kl + RX;
@@ -273,7 +302,9 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
             riemann_hllc_rec(h, ql, qr, rec, fl);
 #pragma unroll
             for (int v = 0; v < 4; ++v) flux[v] = rec[HR_FLUX + v];
-            if (g < TY || j0 + TY == h.ny + 2) {  // the face below cell (i0 + c, j0 + g)
+            // the face below cell (i0 + c, j0 + g); with kCarryOut also the top
+            // row, which the tile above owns but takes over
+            if (g < TY || j0 + TY == h.ny + 2 || (carry & kCarryOut)) {
 #pragma unroll
               for (int e = 0; e < HR_N; ++e) tape->at(tape->fy, e, j0 + g, i0 + c) = rec[e];
               tape->flag(tape->fly, j0 + g, i0 + c) = fl;
@@ -292,6 +323,13 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   }
   __syncthreads();
   after_faces();
+  if (carry & kCarryOut) {  // ring rows RY-2..RY-1 -> rows 0-1 (read by no one until the next face phase)
+    for (int k = tid; k < 12 * 2 * RX; k += NT) {
+      const int pl = k / (2 * RX), e = k - pl * (2 * RX);
+      Real* a = pl < 8 ? sdq + pl * RX * RY : ss + (pl - 8) * RX * RY;
+      a[e] = a[(RY - 2) * RX + e];
+    }
+  }
   if constexpr (TAPE) {
     if (tape->only) return Real(0);
   }
