@@ -118,7 +118,9 @@ int build_worklist(e2d_batch* b) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int res = std::max(1, batch_resident_per_sm<Real>(b->variant));
-  b->grid = std::max(1, std::min(t, sms * res * b->mult));
+  // grid_mult 0: one CTA per tile (no persistent walk, no carry; the hardware
+  // scheduler balances the tiles)
+  b->grid = b->mult == 0 ? std::max(1, t) : std::max(1, std::min(t, sms * res * b->mult));
   if (!b->d_probs) B_CK(cudaMalloc(&b->d_probs, sizeof(BatchProb<double>) * (size_t)b->nprob));
   B_CK(cudaMemcpyAsync(b->d_probs, probs.data(), sizeof(BatchProb<Real>) * (size_t)b->nprob,
                        cudaMemcpyHostToDevice, b->stream));
@@ -385,8 +387,8 @@ int e2d_batch_last_advance_ms(e2d_batch* b, float* ms) {
 
 int e2d_batch_set_schedule(e2d_batch* b, int variant, int grid_mult, int order) {
   if (int rc = check(b)) return rc;
-  if (variant < 0 || variant > 1 || grid_mult < 1 || grid_mult > 64 || order < 0 || order > 1)
-    return bfail(E2D_ERR_INVALID_ARG, "variant 0|1, grid_mult 1..64, order 0|1");
+  if (variant < 0 || variant > 1 || grid_mult < 0 || grid_mult > 64 || order < 0 || order > 1)
+    return bfail(E2D_ERR_INVALID_ARG, "variant 0|1, grid_mult 0..64 (0: one CTA per tile), order 0|1");
   cudaSetDevice(b->device);
   B_CK(cudaStreamSynchronize(b->stream));
   b->variant = variant;
@@ -447,7 +449,7 @@ int e2d_batch_tune(e2d_batch* b, int steps, const char* cache_path, float* best_
   int bv = b->variant, bm = b->mult, bo = b->order;
   int rc = E2D_OK;
   for (int v = 0; v <= 1 && rc == E2D_OK; ++v)
-    for (int m : {1, 2, 3, 4})
+    for (int m : {1, 2, 3, 4, 0})
       for (int o = 0; o <= 1 && rc == E2D_OK; ++o) {
         if ((rc = e2d_batch_set_schedule(b, v, m, o))) break;
         float ms = 0;

@@ -223,7 +223,9 @@ int e2d_batch_download_state(e2d_batch* b, int prob, int which, void* host);
 int e2d_batch_advance(e2d_batch* b, int nStep0, int nsteps, void* dt_log);
 int e2d_batch_last_advance_ms(e2d_batch* b, float* ms);
 /* Schedule: variant 0 = 32x15-cell tiles, 1 = 32x7; grid_mult x resident CTAs
- * per SM x SMs persistent CTAs; order 0 = problem order, 1 = largest first. */
+ * per SM x SMs persistent CTAs, each walking one contiguous run of the tiles
+ * (grid_mult 0: one CTA per tile); order 0 = problem order, 1 = largest
+ * first. */
 int e2d_batch_set_schedule(e2d_batch* b, int variant, int grid_mult, int order);
 int e2d_batch_get_schedule(e2d_batch* b, int* variant, int* grid_mult, int* order, int* grid);
 /* Autotuner: times every schedule on `steps` steps of the current states

@@ -31,8 +31,8 @@ def make_batch(E, prec, riemann):
     return b
 
 
-@pytest.mark.parametrize("schedule", [(0, 1, 0), (0, 2, 1), (1, 1, 1), (1, 4, 0)],
-                         ids=["32x15-x1-order", "32x15-x2-lpt", "32x7-x1-lpt", "32x7-x4-order"])
+@pytest.mark.parametrize("schedule", [(0, 1, 0), (0, 2, 1), (1, 1, 1), (1, 4, 0), (0, 0, 1)],
+                         ids=["32x15-x1-order", "32x15-x2-lpt", "32x7-x1-lpt", "32x7-x4-order", "32x15-pertile-lpt"])
 @pytest.mark.parametrize("riemann", [2, 0], ids=["hllc", "approx"])
 def test_batch_equals_single_runs(e2d, schedule, riemann):
     n = 25
