@@ -35,6 +35,9 @@ namespace {
 // cells at E2D_FUSED_MINB64 CTAs per SM (shared memory and registers must
 // allow that many); FP32: 32 x 15 cells at 4 CTAs per SM (64 registers, 4 x
 // 55 KB of shared memory).  Both need the largest shared-memory carveout.
+#ifndef E2D_FUSED_TX64
+#define E2D_FUSED_TX64 32
+#endif
 #ifndef E2D_FUSED_TY64
 #define E2D_FUSED_TY64 15
 #endif
@@ -45,7 +48,7 @@ namespace {
 #define E2D_FUSED_NT64 256
 #endif
 template <typename Real> struct FusedTile;
-template <> struct FusedTile<double> { using C = TileCfg<double, 32, E2D_FUSED_TY64, E2D_FUSED_NT64>; };
+template <> struct FusedTile<double> { using C = TileCfg<double, E2D_FUSED_TX64, E2D_FUSED_TY64, E2D_FUSED_NT64>; };
 template <> struct FusedTile<float> { using C = TileCfg<float, 32, 15, 256>; };
 
 #ifndef E2D_PREFETCH_CONS

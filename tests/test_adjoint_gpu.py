@@ -151,16 +151,21 @@ def test_adjoint_512_200_steps(e2d, oracle, arith):
     assert max(errs) < FD_TOL, errs
 
 
+@pytest.mark.parametrize("size", [(96, 80), (600, 520)], ids=["96x80", "600x520-carried"])
 @pytest.mark.parametrize("dt_mode", [0, 1], ids=["dt-frozen", "dt-through-max"])
-def test_tape_gives_the_recomputed_gradient(e2d, oracle, monkeypatch, dt_mode, arith):
+def test_tape_gives_the_recomputed_gradient(e2d, oracle, monkeypatch, dt_mode, arith, size):
     """The reverse step reading the forward sweeps' tape (primitives, slopes,
     sources, limiter cases, recorded HLLC solves) gives the gradient of the
     reverse step that recomputes them: the same values enter the same reverse
     arithmetic, so only the order of additions (J, ghost folding, dt
-    adjoint) can differ."""
-    p = e2d.make_params(nx=96, ny=80, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
+    adjoint) can differ.  At 600 x 520 (665 tiles, more than the persistent
+    grid) the taping steps walk runs of tiles up the columns and carry ring
+    rows: the lower tile then records the ring row and y-face row that the
+    tile above no longer computes, which this checks."""
+    nx, ny = size
+    p = e2d.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
                         boundary_type_xmax=2, boundary_type_ymin=3, boundary_type_ymax=3)
-    po = oracle.Params(nx=96, ny=80, gamma0=1.4, cfl=0.8, riemann=2, bc_xmax=2, bc_ymin=3, bc_ymax=3)
+    po = oracle.Params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann=2, bc_xmax=2, bc_ymin=3, bc_ymax=3)
     # (the FMA build's reverse without a tape recomputes its face states in
     # the exact form, a rounding away from its forward's: a state without
     # near-ties keeps the branches the same)

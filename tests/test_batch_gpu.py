@@ -1,5 +1,7 @@
 """The batched ensemble: every problem of a batch is bitwise identical to the
 same problem advanced alone (states and dt sequence), whatever the schedule."""
+import os
+
 import numpy as np
 import pytest
 
@@ -118,4 +120,30 @@ def test_fma_batch_matches_the_oracle(e2d, oracle, prec):
             l1 = [float(np.abs(got[v] - want[v]).sum() / np.abs(want[v]).sum()) for v in range(4)]
             dr = float(np.max(np.abs(dts[:, k].astype(np.float64) - dts_ref) / dts_ref))
             assert max(l1) <= l1_tol and dr <= dt_tol, f"problem {k}: rel L1 {l1}, dt {dr}"
+            assert b.health(k) == 0
+
+
+@pytest.mark.parametrize("schedule", [(0, 1, 0), (1, 2, 1)], ids=["32x15-x1-order", "32x7-x2-lpt"])
+def test_carried_runs_across_problems_match_the_oracle(e2d, oracle, schedule):
+    """An ensemble with many more tiles than CTAs (2244 tiles of 32 x 15 over
+    the persistent grid), so that each CTA walks a run of tiles up the
+    columns of a problem and on into the next problem, the tiles taking over
+    the ring rows and y-face row of the tile below: each problem bitwise
+    equal to the oracle (states and dt), exact build."""
+    sizes = [(1000, 777), (333, 600), (640, 96)]
+    bcs = [[1, 2, 3, 3], [2, 2, 1, 1], [3, 3, 2, 1]]
+    init = ([0.43, 0.6, 0.5], [1.0, 0.3, 0.8], [1.0, 0.9, 0.4], [0.125, 0.7, 0.2],
+            [float(np.float32(0.14)), 0.2, 0.6])
+    n = 8
+    with e2d.Batch(sizes, bcs, gamma0=1.4, cfl=0.8, riemann_solver=2) as b:
+        b.set_schedule(*schedule)
+        b.init_diagonal(*init)
+        dts = b.advance(0, n)
+        for k, ((nx, ny), bc) in enumerate(zip(sizes, bcs)):
+            po = oracle.Params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann=2, bc_xmin=bc[0], bc_xmax=bc[1],
+                               bc_ymin=bc[2], bc_ymax=bc[3])
+            u0 = oracle.init_diagonal(po, *(x[k] for x in init))
+            ref, dts_ref, _, _ = oracle.run(po, n, u0=u0, nthreads=os.cpu_count() or 1)
+            assert np.array_equal(b.final_state(k, n)[:, 2:-2, 2:-2], ref[:, 2:-2, 2:-2]), f"problem {k}"
+            assert np.array_equal(dts[:, k], dts_ref), f"problem {k}"
             assert b.health(k) == 0

@@ -148,3 +148,33 @@ def test_fma_build_small_grids(e2d, oracle, case, version, riemann, mode):
 def test_fma_build_reports_its_arithmetic(e2d):
     assert e2d.arithmetic("exact") == e2d.ARITH_EXACT
     assert e2d.arithmetic("fma") == e2d.ARITH_FMA
+
+
+@pytest.mark.parametrize("mode", ["advance", "percall"])
+@pytest.mark.parametrize("arith", ["exact", "fma"])
+def test_carried_tiles_on_a_ragged_grid(e2d, oracle, arith, mode):
+    """A grid with more tiles than the persistent grid has CTAs (1000 x 777:
+    32 x 52 tiles of 32 x 15, the last row and column ragged), so that every
+    CTA walks a run of tiles that crosses from one column of tiles to the
+    next, and tiles take over the ring rows and y-face row of the tile below
+    (the persistent kernel's carry); reflective and outflow walls in x,
+    periodic in y.  The exact build
+    must give the oracle's bits, the FMA build stay within the specified bar;
+    both with the primitives kept (advance) and through the reference's
+    per-call loop."""
+    nx, ny, n = 1000, 777, 12
+    bc = (1, 2, 3, 3)
+    po = oracle.Params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann=2, bc_xmin=bc[0], bc_xmax=bc[1],
+                       bc_ymin=bc[2], bc_ymax=bc[3])
+    u0 = oracle.init_diagonal(po, 0.43, 1.0, 1.0, 0.125, float(np.float32(0.14)))
+    ref, dts_ref, _, _ = oracle.run(po, n, u0=u0, nthreads=NTHREADS)
+    p = e2d.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
+                        boundary_type_xmin=bc[0], boundary_type_xmax=bc[1], boundary_type_ymin=bc[2],
+                        boundary_type_ymax=bc[3])
+    got, dts = e2d.run_steps(n, p, u0=u0, mode=mode, arith=arith)
+    if arith == "exact":
+        assert np.array_equal(interior(got), interior(ref))
+        assert np.array_equal(np.asarray(dts), dts_ref)
+    else:
+        assert max(rel_l1(got, ref)) <= REL_L1_TOL
+        assert dt_rel(dts, dts_ref) <= DT_REL_TOL
