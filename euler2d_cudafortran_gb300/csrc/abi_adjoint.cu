@@ -48,6 +48,7 @@ struct e2d_adjoint {
   // null when they could not be allocated
   double* qping = nullptr;
   StateMap qmaps[2];
+  StateMap imaps[2];  // the interior tiles of the ping-pong states (the fast step's L2 prefetch)
   std::map<std::tuple<int, double, double, double>, cudaGraphExec_t> fwd_graphs;
   int nchk = 0, kseg = 0, cap_steps = 0;
   bool cap_gradient = false;  // the buffers were laid out for a gradient (tapes considered)
@@ -158,7 +159,8 @@ int ensure(e2d_adjoint* a, int nsteps, bool gradient) {
     A_CK(cudaMemsetAsync(a->pool, 0, (size_t)nstates * a->state_elems * sizeof(double), a->stream));
     a->maps.resize(nstates);
     for (int k = 0; k < nstates; ++k)
-      if (!fused_map_create<double>(a->h, state(a, k), &a->maps[k]))
+      if (!fused_map_create<double>(a->h, state(a, k), &a->maps[k]) ||
+          (k < 2 && !fused_map_create<double>(a->h, state(a, k), &a->imaps[k], true)))
         return afail(E2D_ERR_CUDA, "TMA descriptor setup failed");
     a->kseg = K;
     a->nchk = nchk;
@@ -212,7 +214,7 @@ void enqueue_forward(e2d_adjoint* a, int nsteps, double xc, double yc, double si
       launch_fused_tape(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, tape_of(a, last & 1, k - last * K),
                         s);
     else if (a->qping)
-      launch_fused_map_q(h, a->qmaps[in], state(a, in), state(a, out), qpf(a, out), sd, a->ctl, s);
+      launch_fused_map_q(h, a->qmaps[in], a->imaps[in], state(a, in), state(a, out), qpf(a, out), sd, a->ctl, s);
     else
       launch_fused_map<double>(h, a->maps[in], state(a, in), state(a, out), sd, a->ctl, true, s);
   }

@@ -26,6 +26,7 @@ namespace e2d {
 struct FusedPlan {
   CUtensorMap tm[2];   // [0]: u, [1]: u2
   CUtensorMap tmq[2];  // primitives beside u and u2 (when has_q)
+  CUtensorMap tmi[2];  // the interior tile of u and u2 (the L2 prefetch of what the update reads)
   bool has_q = false;
 };
 
@@ -64,6 +65,14 @@ __device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* tm, int x, in
                    reinterpret_cast<uint64_t>(tm)),
                "r"(x), "r"(y), "r"(0)
                : "memory");
+}
+
+// The tile (i0, j0)'s conservative values, which only the update reads,
+// brought into L2 through an interior map (encode_state_map): x = i0 in FP64,
+// the aligned i0 - 2 in FP32.
+template <typename Real>
+__device__ __forceinline__ void prefetch_cons(const CUtensorMap* tm, int i0, int j0) {
+  prefetch_box_l2(tm, sizeof(Real) == 8 ? i0 : i0 - GW, j0);
 }
 
 // SQ: dx == dy (the shared face source term of tile_compute).  QIN: tm_in
@@ -112,7 +121,7 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
             "r"(smem_u32(base + C::q_off)),
         "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
         : "memory");
-    if (QIN && E2D_PREFETCH_CONS && sizeof(Real) == 4) prefetch_box_l2(&tm_cons, i0 - GW, j0 - GW);
+    if (QIN && E2D_PREFETCH_CONS && sizeof(Real) == 4) prefetch_cons<Real>(&tm_cons, i0, j0);
   }
   const Real dt = sdt[0];
   const bool ok = mbar_wait(bar_a, 0, kTmaWaitCycles);
@@ -264,7 +273,7 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
             "r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(i0 - GW), "r"(j0 - GW), "r"(0), "r"(bar_a)
         : "memory");
-    if (QIN && E2D_PREFETCH_CONS && (sizeof(Real) == 4 || E2D_PREFETCH_CONS64)) prefetch_box_l2(&tm_cons, i0 - GW, j0 - GW);
+    if (QIN && E2D_PREFETCH_CONS && (sizeof(Real) == 4 || E2D_PREFETCH_CONS64)) prefetch_cons<Real>(&tm_cons, i0, j0);
   };
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
@@ -439,15 +448,21 @@ EncodeTiledFn get_encode_fn() {
   return fn;
 }
 
-// 3D map over a pitched state: dims (isize, jsize, 4), zero fill outside.
+// 3D map over a pitched state: dims (isize, jsize, 4), zero fill outside;
+// boxes of the tile with its 2-cell halo, or (interior) of the tile's rows
+// alone -- in FP64 the tile itself (its first column i0 is 16-byte aligned),
+// in FP32 the rows' 36 columns from the aligned column i0 - 2 (the TMA
+// start rule: x times the element size a multiple of 16 bytes).  The
+// interior maps serve prefetch_cons.
 template <typename Real>
-bool encode_state_map(CUtensorMap* tm, const Hydro<Real>& h, Field<Real> f) {
+bool encode_state_map(CUtensorMap* tm, const Hydro<Real>& h, Field<Real> f, bool interior = false) {
   using S = typename FusedTile<Real>::C;
   EncodeTiledFn enc = get_encode_fn();
   if (!enc) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)h.isize, (cuuint64_t)h.jsize, 4};
   const cuuint64_t strides[2] = {(cuuint64_t)f.pitch * sizeof(Real), (cuuint64_t)f.plane * sizeof(Real)};
-  const cuuint32_t box[3] = {(cuuint32_t)S::BXs, (cuuint32_t)S::BYs, 4};
+  const cuuint32_t box[3] = {(cuuint32_t)(interior && sizeof(Real) == 8 ? S::TX : S::BXs),
+                             (cuuint32_t)(interior ? S::TY : S::BYs), 4};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt =
       sizeof(Real) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
@@ -463,8 +478,10 @@ FusedPlan* fused_plan_create(const Hydro<Real>& h, Field<Real> u, Field<Real> u2
   using C = typename FusedTile<Real>::C;
   static_assert(C::BXs * sizeof(Real) % 16 == 0, "TMA inner box must be a multiple of 16 bytes");
   static_assert((C::TX * sizeof(Real)) % 16 == 0, "tile x origin must stay 16-byte aligned");
+  static_assert(sizeof(Real) != 8 || (GW * sizeof(Real)) % 16 == 0, "FP64 interior prefetch starts at column GW");
   FusedPlan* p = new FusedPlan;
-  if (!encode_state_map<Real>(&p->tm[0], h, u) || !encode_state_map<Real>(&p->tm[1], h, u2)) {
+  if (!encode_state_map<Real>(&p->tm[0], h, u) || !encode_state_map<Real>(&p->tm[1], h, u2) ||
+      !encode_state_map<Real>(&p->tmi[0], h, u, true) || !encode_state_map<Real>(&p->tmi[1], h, u2, true)) {
     delete p;
     return nullptr;
   }
@@ -490,20 +507,21 @@ void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Rea
                   StepDt<Real> sd, Ctl* ctl, bool fill_ghosts, cudaStream_t s, const Field<Real>* qout) {
   const CUtensorMap& tmc = plan->tm[in_is_u2 ? 1 : 0];
   if (qout && plan->has_q)
-    launch_fused_tm<Real>(plan->tmq[in_is_u2 ? 1 : 0], tmc, h, in, out, qout, sd, ctl, fill_ghosts, s);
+    launch_fused_tm<Real>(plan->tmq[in_is_u2 ? 1 : 0], plan->tmi[in_is_u2 ? 1 : 0], h, in, out, qout, sd, ctl,
+                          fill_ghosts, s);
   else
     launch_fused_tm<Real>(tmc, tmc, h, in, out, nullptr, sd, ctl, fill_ghosts, s);
 }
 
 template <typename Real>
-bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out) {
+bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out, bool interior) {
   static_assert(sizeof(StateMap) == sizeof(CUtensorMap), "descriptor size");
   using C = typename FusedTile<Real>::C;
   if (!set_fused_attributes<Real>()) {
     cudaGetLastError();
     return false;
   }
-  return encode_state_map<Real>(reinterpret_cast<CUtensorMap*>(out->bytes), h, u);
+  return encode_state_map<Real>(reinterpret_cast<CUtensorMap*>(out->bytes), h, u, interior);
 }
 
 template <typename Real>
@@ -534,14 +552,15 @@ void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double
   else launch_fused_tape_sq<false>(tm, h, in, out, sd, ctl, tape, s);
 }
 
-void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, Field<double> in, Field<double> out,
-                        Field<double> qout, StepDt<double> sd, Ctl* ctl, cudaStream_t s) {
+void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, const StateMap& imap, Field<double> in,
+                        Field<double> out, Field<double> qout, StepDt<double> sd, Ctl* ctl, cudaStream_t s) {
   const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(qmap.bytes);
-  launch_fused_tm<double>(tm, tm, h, in, out, &qout, sd, ctl, true, s);
+  const CUtensorMap& tmi = *reinterpret_cast<const CUtensorMap*>(imap.bytes);
+  launch_fused_tm<double>(tm, tmi, h, in, out, &qout, sd, ctl, true, s);
 }
 
-template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*);
-template bool fused_map_create<float>(const Hydro<float>&, Field<float>, StateMap*);
+template bool fused_map_create<double>(const Hydro<double>&, Field<double>, StateMap*, bool);
+template bool fused_map_create<float>(const Hydro<float>&, Field<float>, StateMap*, bool);
 template void launch_fused_map<double>(const Hydro<double>&, const StateMap&, Field<double>, Field<double>,
                                        StepDt<double>, Ctl*, bool, cudaStream_t);
 template void launch_fused_map<float>(const Hydro<float>&, const StateMap&, Field<float>, Field<float>,

@@ -83,9 +83,11 @@ void fused_plan_destroy(FusedPlan* p);
 template <typename Real> void launch_fused(const Hydro<Real>& h, FusedPlan* plan, int in_is_u2, Field<Real> in,
                                            Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
                                            cudaStream_t s, const Field<Real>* qout = nullptr);
-// A TMA descriptor for any pitched state (used for states outside a run's u/u2).
+// A TMA descriptor for any pitched state (used for states outside a run's u/u2):
+// boxes of a tile with its halo, or (interior) of the tile alone.
 struct StateMap { alignas(64) unsigned char bytes[128]; };
-template <typename Real> bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out);
+template <typename Real>
+bool fused_map_create(const Hydro<Real>& h, Field<Real> u, StateMap* out, bool interior = false);
 // Where a forward step leaves the values of its input state that the reverse
 // step recomputes otherwise (the adjoint's tape): the primitives of every
 // cell, and the slopes and trace source terms of the cells the reverse's
@@ -146,10 +148,11 @@ __host__ __device__ inline TapeOut tape_at(double* base, int j, long long plane,
 void launch_fused_tape(const Hydro<double>& h, const StateMap& map, Field<double> in, Field<double> out,
                        StepDt<double> sd, Ctl* ctl, const TapeOut& tape, cudaStream_t s);
 // The step with primitives kept beside the states (as the run's advance):
-// qmap maps the input's primitives (current, ghosts and corners included);
-// the output's go to qout.  Ghosts of the output are filled.
-void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, Field<double> in, Field<double> out,
-                        Field<double> qout, StepDt<double> sd, Ctl* ctl, cudaStream_t s);
+// qmap maps the input's primitives (current, ghosts and corners included),
+// imap the interior tiles of the input state (prefetched into L2 for the
+// update); the output's primitives go to qout.  Ghosts of the output are filled.
+void launch_fused_map_q(const Hydro<double>& h, const StateMap& qmap, const StateMap& imap, Field<double> in,
+                        Field<double> out, Field<double> qout, StepDt<double> sd, Ctl* ctl, cudaStream_t s);
 template <typename Real> void launch_fused_map(const Hydro<Real>& h, const StateMap& map, Field<Real> in,
                                                Field<Real> out, StepDt<Real> sd, Ctl* ctl, bool fill_ghosts,
                                                cudaStream_t s);
