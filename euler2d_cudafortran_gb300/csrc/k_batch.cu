@@ -2,12 +2,14 @@
 // problems of uneven sizes by one time step.
 //
 // The tiles of every problem form one flattened work list (problem p owns
-// tiles [tile_begin[p], tile_begin[p+1])); a persistent grid of CTAs walks
-// the list with a fixed stride.  Each tile is computed exactly as in the
-// single-run kernel (tile.cuh) with its own problem's parameters, its own dt
-// (from the problem's running CFL maximum) and its own ghost rules, and
-// folds the next step's CFL maximum into the problem's own slot.  The box is
-// loaded with coalesced plain loads because every problem has its own array.
+// tiles [tile_begin[p], tile_begin[p+1]), column by column); a persistent
+// grid of CTAs splits the list into contiguous runs, one per CTA.  Each tile
+// is computed exactly as in the single-run kernel (tile.cuh) with its own
+// problem's parameters, its own dt (from the problem's running CFL maximum)
+// and its own ghost rules, and folds the next step's CFL maximum into the
+// problem's own slot.  Boxes are copied with 16-byte asynchronous copies
+// because every problem has its own array (a tensor map per problem would be
+// a kernel argument per problem).
 #include <algorithm>
 
 #include "batch.h"
