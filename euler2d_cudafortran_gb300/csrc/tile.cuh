@@ -73,8 +73,8 @@ __device__ __forceinline__ bool owns(int g, int t0, int w, int n) {
 // box_src (optional): where the conservative box was loaded, when not in
 // place at q_off (it is then read into q_off); after_faces: run by every
 // thread right after the barrier that ends the face phase, after which no
-// phase reads the box, the slopes or the sources (a persistent caller loads
-// the next box into the box region there).
+// phase reads the box (a persistent caller loads the next box into the box
+// region there; the carry below copies two ring rows of slopes and sources).
 // SQ (only when dx == dy, so that dtdx == dtdy bit for bit): the source term
 // of a face state, (s*dtdx)*0.5, is the same for the four faces of a cell;
 // the ring pass forms it once and stores it in place of s.
