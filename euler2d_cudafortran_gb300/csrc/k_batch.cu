@@ -143,8 +143,7 @@ __global__ void __launch_bounds__(C::NT, MINB)
     const bool only = TAPE && P.tape.only;  // a tape-only pass: no update, no dt
     Real m = tile_compute<Real, C, SQ, QIN, TAPE>(sh, base, face_counter, red, i0, j0, in, out, qout, sdt[1],
                                                   sdt[2], true, wr >= 0 && !only, &ctls[id].health,
-                                                  nullptr, prefetch, &P.tape, find_next,
-                                                  carry);
+                                                  prefetch, &P.tape, find_next, carry);
     if (tid == 0 && !only) {
       if (stile == 0) {
         if (dt_log) dt_log[id] = sdt[0];

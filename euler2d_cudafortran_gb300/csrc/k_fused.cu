@@ -191,8 +191,7 @@ __global__ void __launch_bounds__(E2D_FUSED_NT64, E2D_FUSED_MINB64)
   }
   const bool want_dt = sd.wr_slot >= 0 && !tape.only;
   double m = tile_compute<double, C, SQ, false, true>(h, base, face_counter, red, i0, j0, in, out, out, sdt[1],
-                                                      sdt[2], true, want_dt, &ctl->health, nullptr, NoHook(),
-                                                      &tape);
+                                                      sdt[2], true, want_dt, &ctl->health, NoHook(), &tape);
   if (tid == 0 && !tape.only) {
     if (blockIdx.x == 0 && blockIdx.y == 0) {
       if (sd.dt_log) sd.dt_log[sd.log_index] = dt;
@@ -309,8 +308,7 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? E2D_FUSED_NT64 : 256, size
                           : 0;
     const Real m = tile_compute<Real, C, SQ, QIN, TAPE>(h, base, face_counter, red, i0, j0, in, out, qout,
                                                         sdt[1], sdt[2], fill_ghosts != 0, want_dt, &ctl->health,
-                                                        nullptr, prefetch, TAPE ? &tape : nullptr, NoHook(),
-                                                        carry);
+                                                        prefetch, TAPE ? &tape : nullptr, NoHook(), carry);
     if (tid == 0) {
       mmax = Ops<Real>::max(mmax, m);
       *face_counter = 0;

@@ -70,9 +70,7 @@ __device__ __forceinline__ bool owns(int g, int t0, int w, int n) {
   return (g >= t0 && g < end) || (t0 == GW && g < GW) || (t0 + w >= n + GW && g >= n + GW);
 }
 
-// box_src (optional): where the conservative box was loaded, when not in
-// place at q_off (it is then read into q_off); after_faces: run by every
-// thread right after the barrier that ends the face phase, after which no
+// after_faces: run by every thread right after the barrier that ends the face phase, after which no
 // phase reads the box (a persistent caller loads the next box into the box
 // region there; the carry below copies two ring rows of slopes and sources).
 // SQ (only when dx == dy, so that dtdx == dtdy bit for bit): the source term
@@ -104,7 +102,7 @@ template <typename Real, class C, bool SQ = false, bool QIN = false, bool TAPE =
 __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, int* face_counter, Real* red,
                                              int i0, int j0, const Field<Real>& in, const Field<Real>& out,
                                              const Field<Real>& qout, Real dtdx, Real dtdy, bool fill_ghosts,
-                                             bool want_dt, unsigned* health, const Real* box_src = nullptr,
+                                             bool want_dt, unsigned* health,
                                              Hook after_faces = Hook(), const TapeOut* tape = nullptr,
                                              Hook2 before_faces = Hook2(), int carry = 0) {
   static_assert(!TAPE || (sizeof(Real) == 8 && !QIN), "the tape is written by the FP64 conversion path");
@@ -120,14 +118,12 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
   // and applies dt/dx once per cell in the update, fused with the addition.
   constexpr bool kFluxRaw = SQ && E2D_FMA_FORMS;
 
-  // ---- primitives of the whole box (computePrimitives), in place unless
-  // the box was loaded elsewhere
+  // ---- primitives of the whole box (computePrimitives), in place
   if constexpr (!QIN) {
-    const Real* src = box_src ? box_src : sq;
     for (int k = tid; k < BXs * BYs; k += NT) {
       Real u[4], q[4];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) u[v] = src[v * BXs * BYs + k];
+      for (int v = 0; v < 4; ++v) u[v] = sq[v * BXs * BYs + k];
       primitives(h, u, q);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sq[v * BXs * BYs + k] = q[v];
