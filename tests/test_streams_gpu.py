@@ -92,12 +92,17 @@ def test_percall_steps_see_an_uploaded_state(e2d, prec):
     assert np.array_equal(ua, ub)
 
 
+@pytest.mark.parametrize("size", [(96, 80), (700, 610)], ids=["96x80", "700x610-carried"])
 @pytest.mark.parametrize("prec", [8, 4], ids=["f64", "f32"])
-def test_kept_primitives_change_no_bit(e2d, monkeypatch, prec):
+def test_kept_primitives_change_no_bit(e2d, monkeypatch, prec, size):
     """implementationVersion 0 keeps the primitives of its states beside them
     (each step writes its output's); with E2D_KEEP_PRIMS=0 every step
-    converts its box instead.  Both give the same states and dt."""
-    p = _params(e2d, 0, prec)
+    converts its box instead.  Both give the same states and dt -- at 700 x
+    610 also with the persistent kernel's carried ring rows (902 tiles), on
+    primitive and on conservative boxes."""
+    nx, ny = size
+    p = e2d.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC, precision=prec,
+                        boundary_type_xmax=2, boundary_type_ymin=3, boundary_type_ymax=3)
     runs = []
     for keep in ("1", "0"):
         monkeypatch.setenv("E2D_KEEP_PRIMS", keep)

@@ -115,12 +115,15 @@ def test_noalloc_rejects_overlapping_or_oversized_layouts(e2d):
 
 
 @pytest.mark.gpu
-def test_noalloc_on_caller_arrays_with_a_wider_pitch(e2d):
+@pytest.mark.parametrize("nx,ny,extra", [(70, 52, 13), (700, 610, 5)], ids=["70x52", "700x610-carried"])
+def test_noalloc_on_caller_arrays_with_a_wider_pitch(e2d, nx, ny, extra):
     """Arrays the caller allocated (torch) with a row pitch wider than nx+4:
     two calls give the regular step's interiors bit for bit, and the output's
-    ghost cells keep what the caller put there."""
+    ghost cells keep what the caller put there.  At 700 x 610 the regular
+    (fused) step it is compared with walks runs of its 902 tiles with the
+    carried ring rows, while this step stores fluxes: two independent
+    formulations of the same arithmetic."""
     torch = pytest.importorskip("torch")
-    nx, ny, extra = 70, 52, 13
     p = e2d.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC, precision=8)
     lib = e2d.load_library()
     with e2d.HydroRun(p) as ref:
