@@ -615,8 +615,10 @@ def selftest_wait(limit_cycles: int = 1 << 24):
 def selftest_arith(op: int, mode: int, n: int, seed: int = 1, rates: bool = False):
     """Bitwise check of the integer-pipe division (op 0) / square root (op 1)
     against the hardware, or of the exponent-test pressure floor (op 2) and
-    limiter sign test (op 3) against the product (and maximum), on n inputs;
-    returns (mismatches, first_bad[4], rates)."""
+    limiter sign test (op 3) against the product (and maximum), or of the
+    faithful division (op 4) / square root (op 5) to within one neighbour of
+    the hardware result, on n inputs; returns (mismatches, first_bad[4],
+    rates)."""
     bad = ctypes.c_ulonglong()
     first = (ctypes.c_double * 4)()
     em, na = ctypes.c_double(), ctypes.c_double()

@@ -35,7 +35,9 @@ __device__ bool same(double x, double y) {
   return a == b;
 }
 
-// op 0: division, op 1: square root, op 2: the pressure floor max(a, b*c)
+// op 0: division, op 1: square root (both bit for bit), op 4 / op 5: the
+// faithful division and square root (equal to the hardware result or one of
+// its two neighbours), op 2: the pressure floor max(a, b*c)
 // (against the emulated maximum of the hardware product), op 3: the
 // limiter's sign test dlft*drgt <= 0 from signs and exponents (the product
 // taken where it reports the undecided band), against the product (mode 3:
@@ -89,6 +91,8 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       }
       continue;
     }
+    const bool faithful = op >= 4;
+    const int bop = faithful ? op - 4 : op;  // 0: division, 1: square root
     if (mode < 3) {
       a = rand_double(r1, mode);
       b = rand_double(r2, mode);
@@ -96,8 +100,8 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       a = (r1 & 4) ? 0.0 : (double)(int)((r1 >> 8) & 7);
       a = (r1 & 1) ? -a : a;
       b = rand_double(r2, (r2 & 1) ? 0 : 2);
-      if (op == 1) a = (r1 & 4) ? a : (double)((r1 >> 8) & 7);
-    } else if (op == 0) {
+      if (bop == 1) a = (r1 & 4) ? a : (double)((r1 >> 8) & 7);
+    } else if (bop == 0) {
       b = rand_double(r2, 1);
       const double q = rand_double(r1, 1);
       const double qm = q + 0.5 * (__longlong_as_double(__double_as_longlong(q) + 1) - q);  // rounds to a neighbour
@@ -109,9 +113,15 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       a = __dmul_rn(q + h, q + h);
       a = __longlong_as_double(__double_as_longlong(a) + (long long)(r2 & 3) - 1);
     }
-    const double x = op == 0 ? e2d::emul::div_rn(a, b) : e2d::emul::sqrt_rn(a);
-    const double y = op == 0 ? __ddiv_rn(a, b) : __dsqrt_rn(a);
-    if (!same(x, y)) {
+    const double x = bop == 0 ? (faithful ? e2d::emul::div_fa(a, b) : e2d::emul::div_rn(a, b))
+                              : (faithful ? e2d::emul::sqrt_fa(a) : e2d::emul::sqrt_rn(a));
+    const double y = bop == 0 ? __ddiv_rn(a, b) : __dsqrt_rn(a);
+    bool ok = same(x, y);
+    if (!ok && faithful) {  // a neighbour of the correctly rounded result: patterns one apart, same sign
+      const long long ix = __double_as_longlong(x), iy = __double_as_longlong(y);
+      ok = x == x && y == y && (ix ^ iy) >= 0 && (ix - iy == 1 || iy - ix == 1);
+    }
+    if (!ok) {
       if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
     }
   }
@@ -121,7 +131,13 @@ __global__ void k_rate(int op, int emulated, int iters, double* out) {
   double x0 = 1.0 + threadIdx.x * 1e-3, x1 = x0 + 0.25, x2 = x0 + 0.5, x3 = x0 + 0.75;
   const double c = 0.999;
   for (int i = 0; i < iters; ++i) {
-    if (op == 0) {
+    if (op == 4 && emulated) {
+      x0 = e2d::emul::div_fa(c, x0) + 1.0; x1 = e2d::emul::div_fa(c, x1) + 1.0;
+      x2 = e2d::emul::div_fa(c, x2) + 1.0; x3 = e2d::emul::div_fa(c, x3) + 1.0;
+    } else if (op == 5 && emulated) {
+      x0 = e2d::emul::sqrt_fa(x0) + 1.0; x1 = e2d::emul::sqrt_fa(x1) + 1.0;
+      x2 = e2d::emul::sqrt_fa(x2) + 1.0; x3 = e2d::emul::sqrt_fa(x3) + 1.0;
+    } else if (op == 0 || op == 4) {
       if (emulated) {
         x0 = e2d::emul::div_rn(c, x0) + 1.0; x1 = e2d::emul::div_rn(c, x1) + 1.0;
         x2 = e2d::emul::div_rn(c, x2) + 1.0; x3 = e2d::emul::div_rn(c, x3) + 1.0;
@@ -185,7 +201,7 @@ extern "C" int e2d_selftest_wait(long long limit_cycles, int* arrived_completed,
 extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* first_bad, double* emulated_per_s,
                                   double* native_per_s) {
-  if (op < 0 || op > 3 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
+  if (op < 0 || op > 5 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
@@ -209,7 +225,7 @@ extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long l
   k_check<<<blocks, threads>>>(op, mode, n, seed, d_bad, d_first);
   cudaMemcpy(mismatches, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   if (first_bad) cudaMemcpy(first_bad, d_first, 4 * sizeof(double), cudaMemcpyDeviceToHost);
-  if (emulated_per_s && native_per_s && op < 2) {
+  if (emulated_per_s && native_per_s && (op < 2 || op > 3)) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

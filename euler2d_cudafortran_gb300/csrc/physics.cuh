@@ -9,9 +9,10 @@
 //
 // The library's second build (-fmad=true, E2D_FMA=1) contracts multiply-adds
 // and, where E2D_FMA_FORMS marks it, writes a few expressions in forms that
-// fuse better (fewer FP64 instructions, different rounding): its results
-// agree with serial_ref to the specified 1e-12 relative L1 and 1e-14 relative
-// dt instead of bit for bit.
+// fuse better (fewer FP64 instructions, different rounding), and rounds its
+// double divisions and square roots faithfully: its results agree with
+// serial_ref to the specified 1e-12 relative L1 and 1e-14 relative dt instead
+// of bit for bit.
 //
 // Real = double (fp_kind = dp_kind) or float (fp_kind = sp_kind).  Fortran
 // default-real literals stay single precision in both builds:
@@ -34,6 +35,13 @@
 #define E2D_FMA_FORMS 1
 #else
 #define E2D_FMA_FORMS 0
+#endif
+// The FMA build's double division and square root are faithfully rounded
+// (emul::div_fa, emul::sqrt_fa: within one unit in the last place, a dozen
+// fewer integer instructions on their dependent chains); the exact build's
+// round to nearest, as IEEE.
+#ifndef E2D_FAITHFUL_DIVSQRT
+#define E2D_FAITHFUL_DIVSQRT E2D_FMA_FORMS
 #endif
 
 namespace e2d {
@@ -98,8 +106,13 @@ struct Ops<double> {
 #else
 template <>
 struct Ops<double> {
+#if E2D_FAITHFUL_DIVSQRT
+  static __device__ __forceinline__ double div(double a, double b) { return emul::div_fa(a, b); }
+  static __device__ __forceinline__ double sqrt(double a) { return emul::sqrt_fa(a); }
+#else
   static __device__ __forceinline__ double div(double a, double b) { return emul::div_rn(a, b); }
   static __device__ __forceinline__ double sqrt(double a) { return emul::sqrt_rn(a); }
+#endif
   static __device__ __forceinline__ double max(double a, double b) { return emul::max_i(a, b); }
   static __device__ __forceinline__ double min(double a, double b) { return emul::min_i(a, b); }
   static __device__ __forceinline__ bool gt0(double x) { return emul::gt0(x); }
