@@ -21,10 +21,11 @@ Two builds of the same sources share one C ABI:
     ``-fmad=true``: a multiplication feeding an addition is one fused
     multiply-add, one rounding instead of two and one FP64 issue slot instead
     of two -- what nvfortran's ``-O3 -cuda`` / ``-stdpar=gpu`` builds of the
-    reference do by default (cuf/Makefile:22, stdpar/Makefile:8).  Division and
-    square root stay correctly rounded; results agree with the oracle to the
-    specified 1e-12 relative L1 per variable and 1e-14 relative dt, not bit for
-    bit.
+    reference do by default (cuf/Makefile:22, stdpar/Makefile:8).  Double
+    division and square root are faithfully rounded (the correctly rounded
+    result or one of its two neighbours; single precision stays IEEE); results
+    agree with the oracle to the specified 1e-12 relative L1 per variable and
+    1e-14 relative dt, not bit for bit.
 """
 from __future__ import annotations
 
