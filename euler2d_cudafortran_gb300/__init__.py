@@ -616,9 +616,9 @@ def selftest_arith(op: int, mode: int, n: int, seed: int = 1, rates: bool = Fals
     """Bitwise check of the integer-pipe division (op 0) / square root (op 1)
     against the hardware, or of the exponent-test pressure floor (op 2) and
     limiter sign test (op 3) against the product (and maximum), or of the
-    faithful division (op 4) / square root (op 5) to within one neighbour of
-    the hardware result, on n inputs; returns (mismatches, first_bad[4],
-    rates)."""
+    faithful division (op 4; single precision op 6) / square root (op 5; op 7)
+    to within one neighbour of the hardware result, on n inputs; returns
+    (mismatches, first_bad[4], rates)."""
     bad = ctypes.c_ulonglong()
     first = (ctypes.c_double * 4)()
     em, na = ctypes.c_double(), ctypes.c_double()

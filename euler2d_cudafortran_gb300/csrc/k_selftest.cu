@@ -37,7 +37,8 @@ __device__ bool same(double x, double y) {
 
 // op 0: division, op 1: square root (both bit for bit), op 4 / op 5: the
 // faithful division and square root (equal to the hardware result or one of
-// its two neighbours), op 2: the pressure floor max(a, b*c)
+// its two neighbours), op 6 / op 7: the same for single precision, op 2: the
+// pressure floor max(a, b*c)
 // (against the emulated maximum of the hardware product), op 3: the
 // limiter's sign test dlft*drgt <= 0 from signs and exponents (the product
 // taken where it reports the undecided band), against the product (mode 3:
@@ -88,6 +89,40 @@ __global__ void k_check(int op, int mode, long long n, uint64_t seed, unsigned l
       const bool y = __dmul_rn(a, b) <= 0.0;
       if (x != y) {
         if (atomicAdd(bad, 1ull) == 0) { first[0] = a; first[1] = b; first[2] = x; first[3] = y; }
+      }
+      continue;
+    }
+    if (op >= 6) {  // single precision, faithful: 6 division, 7 square root
+      float fa, fb = 1.0f;
+      if (mode == 0) {
+        fa = __uint_as_float((unsigned)r1); fb = __uint_as_float((unsigned)r2);
+      } else if (mode == 1 || mode == 2) {  // exponents within +-20 (1) or +-100 (2) of 1
+        const unsigned span = mode == 1 ? 20u : 100u;
+        fa = __uint_as_float(((unsigned)r1 & 0x807fffffu) | ((127u - span + (unsigned)((r1 >> 40) % (2 * span + 1))) << 23));
+        fb = __uint_as_float(((unsigned)r2 & 0x807fffffu) | ((127u - span + (unsigned)((r2 >> 40) % (2 * span + 1))) << 23));
+      } else if (mode == 4) {  // signed zeros and small integers over random denominators
+        fa = (r1 & 4) ? 0.0f : (float)(int)((r1 >> 8) & 7);
+        fa = (r1 & 1) ? -fa : fa;
+        fb = __uint_as_float(((unsigned)r2 & 0x807fffffu) | ((107u + (unsigned)((r2 >> 40) % 41)) << 23));
+        if (op == 7) fa = fabsf(fa);
+      } else {  // results next to a rounding boundary
+        const float q = __uint_as_float(((unsigned)r1 & 0x007fffffu) | ((117u + (unsigned)((r1 >> 40) % 21)) << 23));
+        const float h = 0.5f * (__uint_as_float(__float_as_uint(q) + 1) - q);
+        if (op == 6) {
+          fb = __uint_as_float(((unsigned)r2 & 0x807fffffu) | ((117u + (unsigned)((r2 >> 40) % 21)) << 23));
+          fa = (float)((double)(q + h) * (double)fb);  // (q + half an ulp) * b, rounded once to float
+        } else {
+          fa = (float)((double)q * (double)q + (double)q * (double)(2.0f * h));  // ~ (q + h)^2
+        }
+        fa = __uint_as_float(__float_as_uint(fa) + (unsigned)(r2 & 3) - 1u);
+      }
+      const float fx = op == 6 ? e2d::emul::fdiv_fa(fa, fb) : e2d::emul::fsqrt_fa(fa);
+      const float fy = op == 6 ? __fdiv_rn(fa, fb) : __fsqrt_rn(fa);
+      const unsigned ix = __float_as_uint(fx), iy = __float_as_uint(fy);
+      const bool ok = ix == iy || (fx != fx && fy != fy) ||
+                      (fx == fx && fy == fy && ((ix ^ iy) >> 31) == 0 && (ix - iy == 1u || iy - ix == 1u));
+      if (!ok) {
+        if (atomicAdd(bad, 1ull) == 0) { first[0] = fa; first[1] = fb; first[2] = fx; first[3] = fy; }
       }
       continue;
     }
@@ -201,7 +236,7 @@ extern "C" int e2d_selftest_wait(long long limit_cycles, int* arrived_completed,
 extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* first_bad, double* emulated_per_s,
                                   double* native_per_s) {
-  if (op < 0 || op > 5 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
+  if (op < 0 || op > 7 || mode < 0 || mode > 4 || n < 0 || !mismatches) return E2D_ERR_INVALID_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
@@ -225,7 +260,7 @@ extern "C" int e2d_selftest_arith(int op, int mode, long long n, unsigned long l
   k_check<<<blocks, threads>>>(op, mode, n, seed, d_bad, d_first);
   cudaMemcpy(mismatches, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   if (first_bad) cudaMemcpy(first_bad, d_first, 4 * sizeof(double), cudaMemcpyDeviceToHost);
-  if (emulated_per_s && native_per_s && (op < 2 || op > 3)) {
+  if (emulated_per_s && native_per_s && (op < 2 || op == 4 || op == 5)) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -36,10 +36,11 @@
 #else
 #define E2D_FMA_FORMS 0
 #endif
-// The FMA build's double division and square root are faithfully rounded
-// (emul::div_fa, emul::sqrt_fa: within one unit in the last place, a dozen
-// fewer integer instructions on their dependent chains); the exact build's
-// round to nearest, as IEEE.
+// The FMA build's division and square root are faithfully rounded (double:
+// emul::div_fa, emul::sqrt_fa, a dozen fewer integer instructions on their
+// dependent chains; float: emul::fdiv_fa, emul::fsqrt_fa, a correction of the
+// hardware approximations by one fused residual): within one unit in the last
+// place.  The exact build's round to nearest, as IEEE.
 #ifndef E2D_FAITHFUL_DIVSQRT
 #define E2D_FAITHFUL_DIVSQRT E2D_FMA_FORMS
 #endif
@@ -68,11 +69,18 @@ struct Hydro {
 
 template <typename Real> struct Ops;
 
-// FP32: the hardware operations (the FP32 pipes are not the limit).
+// FP32: the hardware operations (the FP32 pipes are not the limit); in the
+// FMA build, division and square root faithfully rounded (emul::fdiv_fa,
+// emul::fsqrt_fa: a third of the IEEE sequences' instructions).
 template <>
 struct Ops<float> {
+#if E2D_FAITHFUL_DIVSQRT
+  static __device__ __forceinline__ float div(float a, float b) { return emul::fdiv_fa(a, b); }
+  static __device__ __forceinline__ float sqrt(float a) { return emul::fsqrt_fa(a); }
+#else
   static __device__ __forceinline__ float div(float a, float b) { return a / b; }
   static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
+#endif
   static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
   static __device__ __forceinline__ float min(float a, float b) { return fminf(a, b); }
   static __device__ __forceinline__ bool gt0(float x) { return x > 0.0f; }

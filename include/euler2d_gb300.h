@@ -155,11 +155,11 @@ int e2d_measure_fp64_peak(double* dfma_per_s, double* ddiv_per_s);
  * products next to the underflow to zero --, 4 signed zeros and small
  * integers): *mismatches
  * counts results that differ in any bit, first_bad[4] (optional) = a, b,
- * library, reference operation of the first one; ops 4 and 5 check the
- * faithful division and square root of the library's FMA build, which must
- * equal the hardware result or one of its two neighbours.  The two rates
- * (optional, ops 0, 1, 4, 5) are chained operations per second.  Not part of
- * the reference; used by the tests. */
+ * library, reference operation of the first one; ops 4 and 5 (double) and 6
+ * and 7 (single precision) check the faithful division and square root of the
+ * library's FMA build, which must equal the hardware result or one of its two
+ * neighbours.  The two rates (optional, ops 0, 1, 4, 5) are chained
+ * operations per second.  Not part of the reference; used by the tests. */
 int e2d_selftest_arith(int op, int mode, long long n, unsigned long long seed, unsigned long long* mismatches,
                        double* first_bad, double* emulated_per_s, double* native_per_s);
 

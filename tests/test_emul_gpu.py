@@ -9,8 +9,9 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4], ids=["any-bits", "near-1", "wide", "near-boundary", "zeros"])
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5],
-                         ids=["div", "sqrt", "pressure-floor", "limiter-sign", "div-faithful", "sqrt-faithful"])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7],
+                         ids=["div", "sqrt", "pressure-floor", "limiter-sign", "div-faithful", "sqrt-faithful",
+                              "f32-div-faithful", "f32-sqrt-faithful"])
 def test_emulated_matches_hardware(e2d, op, mode):
     bad, first, _ = e2d.selftest_arith(op, mode, 1 << 26, seed=12345 + 17 * mode + op)
     assert bad == 0, f"{bad} mismatches; first (a, b, emulated, hardware) = {first}"
