@@ -71,7 +71,7 @@ template <typename Real> struct Ops;
 
 // FP32: the hardware operations (the FP32 pipes are not the limit); in the
 // FMA build, division and square root faithfully rounded (emul::fdiv_fa,
-// emul::fsqrt_fa: a third of the IEEE sequences' instructions).
+// emul::fsqrt_fa: shorter than the IEEE sequences, no slow path in range).
 template <>
 struct Ops<float> {
 #if E2D_FAITHFUL_DIVSQRT
