@@ -10,10 +10,11 @@ Metric: Mcell-updates/s = nx * ny * steps / time (interior cells; the
 reference's own formula, which counts ghost cells, is reported beside it).
 
 Library build (--arith): "fma" (default; multiply-adds fused as nvfortran's
-GPU builds of the reference do, results within the specified 1e-12 relative
-L1 per variable and 1e-14 relative dt of the FP64 oracle, checked in the
-line's `accuracy_vs_fp64_oracle`) or "exact" (no contraction, bitwise the
-oracle).  Both builds appear in `variants`.
+GPU builds of the reference do, divisions and square roots faithfully
+rounded, results within the specified 1e-12 relative L1 per variable and
+1e-14 relative dt of the FP64 oracle, checked in the line's
+`accuracy_vs_fp64_oracle`) or "exact" (no contraction, IEEE rounding,
+bitwise the oracle).  Both builds appear in `variants`.
 
 value       device time (CUDA events on the launching stream) of `steps`
             steps replayed from a CUDA graph, state resident in HBM.
