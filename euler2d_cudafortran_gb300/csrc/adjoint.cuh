@@ -82,7 +82,7 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
   const double dl = q - qm, dr = qp - q;
   const double dlft = mc ? O::twice(dl) : dl;
   const double drgt = mc ? O::twice(dr) : dr;
-  const double dcen = O::half(qp - qm);
+  const double dcen = slope_centre(qp, qm, dl, dr);
   if (O::le0(dlft * drgt)) return;  // limited to zero
   const bool neg = !O::ge0(dcen);   // dsgn = -1
   const double al = rabs(dlft), ar = rabs(drgt), ac = rabs(dcen);

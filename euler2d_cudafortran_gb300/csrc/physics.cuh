@@ -286,6 +286,19 @@ __device__ __forceinline__ bool prod_le0(double a, double b, bool& amb) {
 #endif
 }
 
+// dcen = 0.5*(qp - qm) of the limiter, from dl = q - qm and dr = qp - q.
+// The FMA build adds dl + dr: the same bits wherever both differences are
+// exact (neighbours within a factor of two of q, by Sterbenz's lemma), and
+// one FP64 addition fewer per slope; the exact build subtracts.
+template <typename Real>
+__device__ __forceinline__ Real slope_centre(Real qp, Real qm, Real dl, Real dr) {
+#if E2D_FMA_FORMS
+  return Ops<Real>::half(dl + dr);
+#else
+  return Ops<Real>::half(qp - qm);
+#endif
+}
+
 // Limiter cases recorded for the adjoint (3 bits per slope): bits 0-1 the
 // selection -- 0 limited to zero, 1 |dlft|, 2 |drgt|, 3 |dcen| -- and bit 2
 // set when the selected one-sided difference has the sign opposite to dcen.
@@ -297,7 +310,7 @@ __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm, bool& 
   const Real dl = q - qm, dr = qp - q;
   const Real dlft = mc ? O::twice(dl) : dl;
   const Real drgt = mc ? O::twice(dr) : dr;
-  const Real dcen = O::half(qp - qm);
+  const Real dcen = slope_centre(qp, qm, dl, dr);
   const Real al = rabs(dlft), ar = rabs(drgt);
   const Real slop = O::min(al, ar);
   bool zero;
@@ -523,6 +536,10 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
 }
 
 // riemann_2d_hllc, serial_ref/m_utils.f90:534-644 (rcsum, unused there, is not formed).
+// The flux samples one side's state (left when SL > 0 or ustar > 0, else
+// right: the reference's four branches), so the kinetic and total energy are
+// formed for that side only, from the same operands: the same bits as the
+// reference's etotl / etotr of the branch taken.
 template <typename Real>
 __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real qleft[4],
                                              const Real qright[4], Real flux[4]) {
@@ -530,26 +547,10 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real rl = O::max(qleft[ID], h.smallr);
   const Real pl = floor_prod(qleft[IP], rl, h.smallp);
   const Real ul = qleft[IU];
-  const Real hrl = O::half(rl);
-#if E2D_FMA_FORMS
-  const Real ecinl = hrl * fmx(ul, ul, qleft[IV] * qleft[IV]);
-#else
-  Real ecinl = (hrl * ul) * ul;
-  ecinl = ecinl + ((hrl * qleft[IV]) * qleft[IV]);
-#endif
-  const Real etotl = (pl * h.entho) + ecinl;
   const Real ptotl = pl;
   const Real rr = O::max(qright[ID], h.smallr);
   const Real pr = floor_prod(qright[IP], rr, h.smallp);
   const Real ur = qright[IU];
-  const Real hrr = O::half(rr);
-#if E2D_FMA_FORMS
-  const Real ecinr = hrr * fmx(ur, ur, qright[IV] * qright[IV]);
-#else
-  Real ecinr = (hrr * ur) * ur;
-  ecinr = ecinr + ((hrr * qright[IV]) * qright[IV]);
-#endif
-  const Real etotr = (pr * h.entho) + ecinr;
   const Real ptotr = pr;
   const Real cfastl = O::sqrt(O::max(O::div(h.gamma0 * pl, rl), h.smallc2));
   const Real cfastr = O::sqrt(O::max(O::div(h.gamma0 * pr, rr), h.smallc2));
@@ -565,40 +566,37 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real ustar = O::div(((rcr * ur) + (rcl * ul)) + (ptotl - ptotr), rcr + rcl);
   const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
 #endif
-  Real ro, uo, ptoto, etoto;
+  // the sampled side (b1 / b2 of the reference: left; b3 / b4: right)
+  const bool b1 = O::gt0(SL), lk = b1 || O::gt0(ustar);
+  const Real rk = lk ? rl : rr, uk = lk ? ul : ur, vk = lk ? qleft[IV] : qright[IV], pk = lk ? pl : pr;
+  const Real hrk = O::half(rk);
 #if E2D_FMA_FORMS
-  // the star states reuse rcl = rl (ul - SL) and rcr = rr (SR - ur):
-  // rl (SL - ul) / (SL - ustar) = rcl / (ustar - SL), and so on.  One star
-  // state, its side chosen by selects: a warp whose faces sample both star
-  // states issues it once.
-  if (O::gt0(SL)) {
-    ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
-  } else if (O::gt0(ustar) || O::gt0(SR)) {
-    const bool lk = O::gt0(ustar);  // the left star state
+  const Real ecink = hrk * fmx(uk, uk, vk * vk);
+#else
+  Real ecink = (hrk * uk) * uk;
+  ecink = ecink + ((hrk * vk) * vk);
+#endif
+  const Real etotk = (pk * h.entho) + ecink;
+  Real ro, uo, ptoto, etoto;
+  if (b1 || !(lk || O::gt0(SR))) {  // supersonic: the side's own state
+    ro = rk; uo = uk; ptoto = pk; etoto = etotk;
+  } else {
+    // the star state of the side, its operands chosen by selects: a warp
+    // whose faces sample both star states issues it once
+    const Real Sk = lk ? SL : SR;
+    uo = ustar; ptoto = ptotstar;
+#if E2D_FMA_FORMS
+    // rl (SL - ul) / (SL - ustar) = rcl / (ustar - SL), and so on
     const Real ps = ptotstar * ustar;
     const Real d = lk ? ustar - SL : SR - ustar;
     ro = O::div(lk ? rcl : rcr, d);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div(fmx(lk ? ul - SL : SR - ur, lk ? etotl : etotr,
-                       fmx(O::neg_if(lk ? ptotl : ptotr, !lk), lk ? ul : ur, O::neg_if(ps, lk))), d);
-  } else {
-    ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
-  }
+    etoto = O::div(fmx(lk ? ul - SL : SR - ur, etotk, fmx(O::neg_if(pk, !lk), uk, O::neg_if(ps, lk))), d);
 #else
-  if (O::gt0(SL)) {
-    ro = rl; uo = ul; ptoto = ptotl; etoto = etotl;
-  } else if (O::gt0(ustar)) {
-    ro = O::div(rl * (SL - ul), SL - ustar);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div((((SL - ul) * etotl) - (ptotl * ul)) + (ptotstar * ustar), SL - ustar);
-  } else if (O::gt0(SR)) {
-    ro = O::div(rr * (SR - ur), SR - ustar);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div((((SR - ur) * etotr) - (ptotr * ur)) + (ptotstar * ustar), SR - ustar);
-  } else {
-    ro = rr; uo = ur; ptoto = ptotr; etoto = etotr;
-  }
+    const Real sk = Sk - uk;
+    ro = O::div(rk * sk, Sk - ustar);
+    etoto = O::div(((sk * etotk) - (pk * uk)) + (ptotstar * ustar), Sk - ustar);
 #endif
+  }
   flux[ID] = ro * uo;
   flux[IU] = ((ro * uo) * uo) + ptoto;
   flux[IP] = (etoto + ptoto) * uo;
