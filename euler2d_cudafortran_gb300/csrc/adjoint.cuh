@@ -173,8 +173,7 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   const double ul = rec[HR_QL + IU], ur = rec[HR_QR + IU], vl = rec[HR_QL + IV], vr = rec[HR_QR + IV];
   const double rl = O::max(rec[HR_QL + ID], h.smallr), rr = O::max(rec[HR_QR + ID], h.smallr);
   const double pl = rec[HR_PL], pr = rec[HR_PR];
-  const double etotl = rec[HR_ETOTL], etotr = rec[HR_ETOTR], cal = rec[HR_CAL], car = rec[HR_CAR];
-  const double cfastl = rec[HR_CFL], cfastr = rec[HR_CFR], SL = rec[HR_SL], SR = rec[HR_SR];
+  const double eK = rec[HR_ETOTK], caC = rec[HR_CA], cfC = rec[HR_CF], SL = rec[HR_SL], SR = rec[HR_SR];
   const double rcl = rec[HR_RCL], rcr = rec[HR_RCR], ustar = rec[HR_USTAR], ptotstar = rec[HR_PSTAR];
   const double ro = rec[HR_RO], etoto = rec[HR_ETOTO], fr = rec[HR_FLUX + ID];
   const bool pl_raw = flags & HF_PL_RAW, pr_raw = flags & HF_PR_RAW;
@@ -182,12 +181,12 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   const bool min_l = flags & HF_MIN_L, max_l = flags & HF_MAX_L, vleft = flags & HF_VLEFT;
   const bool b1 = flags & HF_B1, b2 = flags & HF_B2, b3 = flags & HF_B3;
   const bool star = b2 || b3, lside = b1 || b2;  // sampled side K: left for branches 1, 2
-  const double SK = lside ? SL : SR, rK = lside ? rl : rr, uK = lside ? ul : ur;
-  const double eK = lside ? etotl : etotr, pK = lside ? pl : pr;
+  const double SK = lside ? SL : SR, rK = lside ? rl : rr, uK = lside ? ul : ur, vK = lside ? vl : vr;
+  const double pK = lside ? pl : pr;
   const double uo = star ? ustar : uK, ptoto = star ? ptotstar : pK;
   const double den = rcr + rcl;
 
-  double rlb, rrb, plb, prb, ulb, urb, vlb = 0, vrb = 0, etotlb, etotrb, SLb, SRb, ustarb = 0, ptotstarb = 0;
+  double rlb, rrb, plb, prb, ulb, urb, vlb = 0, vrb = 0, SLb, SRb, ustarb = 0, ptotstarb = 0;
   // flux[IV] = fr * (vl or vr)
   double frb = fb[ID] + fb[IV] * (vleft ? vl : vr);
   if (vleft) vlb += fb[IV] * fr; else vrb += fb[IV] * fr;
@@ -213,10 +212,17 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
       pKb = O::neg_if(nEb * uK, true); uKb -= nEb * pK; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
       SKb += db; ustarb -= db;
     }
+    // etot_K = pK entho + hrK (uK uK + vK vK), hrK = rK / 2 (the other
+    // side's energy is not sampled: its adjoint is zero)
+    pKb += eKb * h.entho;
+    rKb += O::half(eKb) * (uK * uK + vK * vK);
+    const double erK = eKb * rK;  // 2 hrK = rK
+    uKb += erK * uK;
+    const double vKb = erK * vK;
     rlb = lside ? rKb : 0.0; rrb = lside ? 0.0 : rKb;
     ulb = lside ? uKb : 0.0; urb = lside ? 0.0 : uKb;
     plb = lside ? pKb : 0.0; prb = lside ? 0.0 : pKb;
-    etotlb = lside ? eKb : 0.0; etotrb = lside ? 0.0 : eKb;
+    vlb += lside ? vKb : 0.0; vrb += lside ? 0.0 : vKb;
     SLb = lside ? SKb : 0.0; SRb = lside ? 0.0 : SKb;
   }
   // ptotstar and ustar = num / den
@@ -236,24 +242,14 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   const double cmaxb = SRb - SLb;
   if (max_l) ulb += SRb; else urb += SRb;
   if (min_l) ulb += SLb; else urb += SLb;
-  const double cfastlb = cmax_l ? cmaxb : 0.0, cfastrb = cmax_l ? 0.0 : cmaxb;
-  if (cl_act) {
-    const double cab = O::div(cfastlb, O::twice(cfastl));
-    plb += O::div(cab * h.gamma0, rl);
-    rlb -= O::div(cab * cal, rl);
+  // cmax = the faster side C's sound speed sqrt(max(gamma p / rho, smallc2))
+  if (cmax_l ? cl_act : cr_act) {
+    const double rC = cmax_l ? rl : rr;
+    const double cab = O::div(cmaxb, O::twice(cfC));
+    const double pCb = O::div(cab * h.gamma0, rC), rCb = O::div(cab * caC, rC);
+    plb += cmax_l ? pCb : 0.0; prb += cmax_l ? 0.0 : pCb;
+    rlb -= cmax_l ? rCb : 0.0; rrb -= cmax_l ? 0.0 : rCb;
   }
-  if (cr_act) {
-    const double cab = O::div(cfastrb, O::twice(cfastr));
-    prb += O::div(cab * h.gamma0, rr);
-    rrb -= O::div(cab * car, rr);
-  }
-  // etot = p entho + hr u u + hr v v, hr = rho / 2
-  plb += etotlb * h.entho; prb += etotrb * h.entho;
-  rlb += O::half(etotlb) * (ul * ul + vl * vl);
-  rrb += O::half(etotrb) * (ur * ur + vr * vr);
-  const double erl = etotlb * rl, err = etotrb * rr;  // 2 hr = rho
-  ulb += erl * ul; vlb += erl * vl;
-  urb += err * ur; vrb += err * vr;
   // pressure and density floors
   if (pl_raw) qlb[IP] += plb; else rlb += plb * h.smallp;
   if (pr_raw) qrb[IP] += prb; else rrb += prb * h.smallp;

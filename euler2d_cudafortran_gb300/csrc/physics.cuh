@@ -226,6 +226,12 @@ __device__ __forceinline__ void primitives(const Hydro<Real>& h, const Real u[4]
   q[IP] = floor_prod((h.gm1 * q[ID]) * e, q[ID], h.smallp);
 }
 
+// a and b the same number, bit for bit (an integer comparison).
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
+
 // Sound speed of eos (serial_ref/m_utils.f90:27) from primitive q.
 template <typename Real>
 __device__ __forceinline__ Real sound_speed(const Hydro<Real>& h, const Real q[4]) {
@@ -241,6 +247,10 @@ __device__ __forceinline__ Real cell_invdt_q(const Hydro<Real>& h, const Real q[
   const Real c = sound_speed(h, q);
   const Real vx = c + rabs(q[IU]);
   const Real vy = c + rabs(q[IV]);
+#if E2D_FMA_FORMS
+  // square cells: (vx + vy) / dx, one division (the FMA build's form)
+  if (same_bits(h.dx, h.dy)) return O::div(vx + vy, h.dx);
+#endif
   return O::div(vx, h.dx) + O::div(vy, h.dy);
 }
 
@@ -535,6 +545,22 @@ __device__ __forceinline__ void riemann_approx(const Hydro<Real>& h, const Real 
   cmpflx(h, qg, flux);
 }
 
+// The FMA build's HLLC star pressure.  The reference's symmetric form
+// (rcr pl + rcl pr + rcl rcr (ul - ur)) / (rcr + rcl) equals pl + rcl (ul -
+// ustar) for the star velocity ustar = (rcr ur + rcl ul + pl - pr) / (rcr +
+// rcl), identically in rcl, rcr, ul, ur, pl, pr: one fused multiply-add
+// where the symmetric form takes four FP64 operations and a division (the
+// same function, so its derivatives, which the adjoint takes in the
+// symmetric form, are the same).
+template <typename Real>
+__device__ __forceinline__ Real hllc_pstar(Real rcl, Real rcr, Real ul, Real ur, Real pl, Real pr, Real ustar) {
+#ifndef E2D_PSTAR_SYM
+  return fmx(rcl, ul - ustar, pl);
+#else
+  return Ops<Real>::div(fmx(rcr, pl, rcl * fmx(rcr, ul - ur, pr)), rcr + rcl);
+#endif
+}
+
 // riemann_2d_hllc, serial_ref/m_utils.f90:534-644 (rcsum, unused there, is not formed).
 // The flux samples one side's state (left when SL > 0 or ustar > 0, else
 // right: the reference's four branches), so the kinetic and total energy are
@@ -561,7 +587,7 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real rcr = rr * (SR - ur);
 #if E2D_FMA_FORMS
   const Real ustar = O::div(fmx(rcr, ur, fmx(rcl, ul, ptotl - ptotr)), rcr + rcl);
-  const Real ptotstar = O::div(fmx(rcr, ptotl, rcl * fmx(rcr, ul - ur, ptotr)), rcr + rcl);
+  const Real ptotstar = hllc_pstar(rcl, rcr, ul, ur, ptotl, ptotr, ustar);
 #else
   const Real ustar = O::div(((rcr * ur) + (rcl * ul)) + (ptotl - ptotr), rcr + rcl);
   const Real ptotstar = O::div(((rcr * ptotl) + (rcl * ptotr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
@@ -604,10 +630,13 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
 }
 
 // The forward values of one HLLC solve that its reverse needs (the adjoint's
-// face tape), in the order riemann_hllc_rec stores them.
+// face tape), in the order riemann_hllc_rec stores them.  HR_ETOTK is the
+// total energy of the side the flux samples (left for branches 1-2, right
+// for 3-4), HR_CA / HR_CF the sound speed squared and the sound speed of
+// the side that gave cmax: the reverse needs no other side's.
 enum {
-  HR_QL = 0, HR_QR = 4, HR_PL = 8, HR_PR, HR_ETOTL, HR_ETOTR, HR_CAL, HR_CAR, HR_CFL, HR_CFR, HR_SL, HR_SR,
-  HR_RCL, HR_RCR, HR_USTAR, HR_PSTAR, HR_RO, HR_ETOTO, HR_FLUX, HR_N = HR_FLUX + 4
+  HR_QL = 0, HR_QR = 4, HR_PL = 8, HR_PR, HR_ETOTK, HR_CA, HR_CF, HR_SL, HR_SR, HR_RCL, HR_RCR, HR_USTAR,
+  HR_PSTAR, HR_RO, HR_ETOTO, HR_FLUX, HR_N = HR_FLUX + 4
 };
 // flag bits: which operand each max/min, floor and branch of the solve took
 enum {
@@ -627,25 +656,9 @@ __device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const d
   const double rl = O::max(qleft[ID], h.smallr);
   const double pl = floor_pick(qleft[IP], rl, h.smallp, pl_raw);
   const double ul = qleft[IU];
-  const double hrl = O::half(rl);
-#if E2D_FMA_FORMS
-  const double ecinl = hrl * fmx(ul, ul, qleft[IV] * qleft[IV]);
-#else
-  double ecinl = (hrl * ul) * ul;
-  ecinl = ecinl + ((hrl * qleft[IV]) * qleft[IV]);
-#endif
-  const double etotl = (pl * h.entho) + ecinl;
   const double rr = O::max(qright[ID], h.smallr);
   const double pr = floor_pick(qright[IP], rr, h.smallp, pr_raw);
   const double ur = qright[IU];
-  const double hrr = O::half(rr);
-#if E2D_FMA_FORMS
-  const double ecinr = hrr * fmx(ur, ur, qright[IV] * qright[IV]);
-#else
-  double ecinr = (hrr * ur) * ur;
-  ecinr = ecinr + ((hrr * qright[IV]) * qright[IV]);
-#endif
-  const double etotr = (pr * h.entho) + ecinr;
   const double cal = O::div(h.gamma0 * pl, rl), car = O::div(h.gamma0 * pr, rr);
   const bool cl_act = pmax(cal, h.smallc2), cr_act = pmax(car, h.smallc2);
   const double cfastl = O::sqrt(cl_act ? cal : h.smallc2);
@@ -659,50 +672,45 @@ __device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const d
   const double rcr = rr * (SR - ur);
 #if E2D_FMA_FORMS
   const double ustar = O::div(fmx(rcr, ur, fmx(rcl, ul, pl - pr)), rcr + rcl);
-  const double ptotstar = O::div(fmx(rcr, pl, rcl * fmx(rcr, ul - ur, pr)), rcr + rcl);
+  const double ptotstar = hllc_pstar(rcl, rcr, ul, ur, pl, pr, ustar);
 #else
   const double ustar = O::div(((rcr * ur) + (rcl * ul)) + (pl - pr), rcr + rcl);
   const double ptotstar = O::div(((rcr * pl) + (rcl * pr)) + ((rcl * rcr) * (ul - ur)), rcr + rcl);
 #endif
-  double ro, uo, ptoto, etoto;
   const bool b1 = O::gt0(SL), b2 = !b1 && O::gt0(ustar), b3 = !b1 && !b2 && O::gt0(SR);
+  const bool lk = b1 || b2;  // the sampled side
+  const double rk = lk ? rl : rr, uk = lk ? ul : ur, vk = lk ? qleft[IV] : qright[IV], pk = lk ? pl : pr;
+  const double hrk = O::half(rk);
 #if E2D_FMA_FORMS
-  if (b1) {
-    ro = rl; uo = ul; ptoto = pl; etoto = etotl;
-  } else if (b2) {
-    const double d = ustar - SL;
-    ro = O::div(rcl, d);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div(fmx(ul - SL, etotl, fmx(pl, ul, -(ptotstar * ustar))), d);
-  } else if (b3) {
-    const double d = SR - ustar;
-    ro = O::div(rcr, d);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div(fmx(SR - ur, etotr, fmx(-pr, ur, ptotstar * ustar)), d);
-  } else {
-    ro = rr; uo = ur; ptoto = pr; etoto = etotr;
-  }
+  const double ecink = hrk * fmx(uk, uk, vk * vk);
 #else
-  if (b1) {
-    ro = rl; uo = ul; ptoto = pl; etoto = etotl;
-  } else if (b2) {
-    ro = O::div(rl * (SL - ul), SL - ustar);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div((((SL - ul) * etotl) - (pl * ul)) + (ptotstar * ustar), SL - ustar);
-  } else if (b3) {
-    ro = O::div(rr * (SR - ur), SR - ustar);
-    uo = ustar; ptoto = ptotstar;
-    etoto = O::div((((SR - ur) * etotr) - (pr * ur)) + (ptotstar * ustar), SR - ustar);
-  } else {
-    ro = rr; uo = ur; ptoto = pr; etoto = etotr;
-  }
+  double ecink = (hrk * uk) * uk;
+  ecink = ecink + ((hrk * vk) * vk);
 #endif
+  const double etotk = (pk * h.entho) + ecink;
+  double ro, uo, ptoto, etoto;
+  if (!(b2 || b3)) {
+    ro = rk; uo = uk; ptoto = pk; etoto = etotk;
+  } else {
+    const double Sk = lk ? SL : SR;
+    uo = ustar; ptoto = ptotstar;
+#if E2D_FMA_FORMS
+    const double ps = ptotstar * ustar;
+    const double d = lk ? ustar - SL : SR - ustar;
+    ro = O::div(lk ? rcl : rcr, d);
+    etoto = O::div(fmx(lk ? ul - SL : SR - ur, etotk, fmx(O::neg_if(pk, !lk), uk, O::neg_if(ps, lk))), d);
+#else
+    const double sk = Sk - uk;
+    ro = O::div(rk * sk, Sk - ustar);
+    etoto = O::div(((sk * etotk) - (pk * uk)) + (ptotstar * ustar), Sk - ustar);
+#endif
+  }
   const double f0 = ro * uo;
   const bool vleft = O::gt0(f0);
 #pragma unroll
   for (int v = 0; v < 4; ++v) { rec[HR_QL + v] = qleft[v]; rec[HR_QR + v] = qright[v]; }
-  rec[HR_PL] = pl; rec[HR_PR] = pr; rec[HR_ETOTL] = etotl; rec[HR_ETOTR] = etotr;
-  rec[HR_CAL] = cal; rec[HR_CAR] = car; rec[HR_CFL] = cfastl; rec[HR_CFR] = cfastr;
+  rec[HR_PL] = pl; rec[HR_PR] = pr; rec[HR_ETOTK] = etotk;
+  rec[HR_CA] = cmax_l ? cal : car; rec[HR_CF] = cmax;
   rec[HR_SL] = SL; rec[HR_SR] = SR; rec[HR_RCL] = rcl; rec[HR_RCR] = rcr;
   rec[HR_USTAR] = ustar; rec[HR_PSTAR] = ptotstar; rec[HR_RO] = ro; rec[HR_ETOTO] = etoto;
   rec[HR_FLUX + ID] = f0;
