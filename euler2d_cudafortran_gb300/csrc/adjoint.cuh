@@ -24,17 +24,20 @@ __device__ __forceinline__ bool picks_first_min(double a, double b) { return emu
 
 // computePrimitives (serial_ref/m_utils.f90:35-64) reverse: qb (adjoint of
 // r, p, u, v) -> ub (adjoint of rho, E, rho u, rho v), given the forward
-// primitives q of the same cell (r = q[ID], u = q[IU], v = q[IV]).
+// primitives q of the same cell (all four: r = q[ID], p = q[IP], u = q[IU],
+// v = q[IV]).  eos's pressure max((gm1 r) e, r smallp), e = E/r - eken,
+// returned its first operand exactly when p > r smallp (it returned p; the
+// floor would give p == r smallp), decided like floor_pick; unfloored,
+// dp/dr = gm1 e = p / r and dp/de = gm1 r.
 __device__ __forceinline__ void primitives_rev_q(const Hydro<double>& h, const double u[4], const double q[4],
                                                  const double qb[4], double ub[4]) {
   const double r = q[ID], uu = q[IU], vv = q[IV];
-  const double eken = O::half(uu * uu + vv * vv);
   const double eu = O::div(u[IP], r);
-  const double e = eu - eken;
-  const double pa = (h.gm1 * r) * e, pb = r * h.smallp;
+  bool raw;
+  (void)floor_pick(q[IP], r, h.smallp, raw);
   double rb = qb[ID], eb = 0.0;
-  if (picks_first_max(pa, pb)) {
-    rb += qb[IP] * h.gm1 * e;
+  if (raw) {
+    rb += qb[IP] * O::div(q[IP], r);
     eb = qb[IP] * h.gm1 * r;
   } else {
     rb += qb[IP] * h.smallp;
@@ -54,8 +57,8 @@ __device__ __forceinline__ void primitives_rev_q(const Hydro<double>& h, const d
 // The same, recomputing the primitives from u.
 __device__ __forceinline__ void primitives_rev(const Hydro<double>& h, const double u[4], const double qb[4],
                                                double ub[4]) {
-  const double r = O::max(u[ID], h.smallr);
-  const double q[4] = {r, 0.0, O::div(u[IU], r), O::div(u[IV], r)};  // ID, IP (unused), IU, IV
+  double q[4];
+  primitives(h, u, q);
   primitives_rev_q(h, u, q, qb, ub);
 }
 
@@ -82,7 +85,7 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
   const double dl = q - qm, dr = qp - q;
   const double dlft = mc ? O::twice(dl) : dl;
   const double drgt = mc ? O::twice(dr) : dr;
-  const double dcen = slope_centre(qp, qm, dl, dr);
+  const double dcen = O::half(qp - qm);
   if (O::le0(dlft * drgt)) return;  // limited to zero
   const bool neg = !O::ge0(dcen);   // dsgn = -1
   const double al = rabs(dlft), ar = rabs(drgt), ac = rabs(dcen);

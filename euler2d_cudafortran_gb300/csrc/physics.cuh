@@ -217,13 +217,16 @@ __device__ __forceinline__ void primitives(const Hydro<Real>& h, const Real u[4]
   q[IV] = O::div(u[IV], q[ID]);
 #if E2D_FMA_FORMS
   // a sum of two products written as one fused form, so that every kernel
-  // rounds it alike (contraction alone may fuse either product)
+  // rounds it alike (contraction alone may fuse either product); then
+  // (gm1 rho) (E / rho - eken) as gm1 (E - rho eken): one fused form and a
+  // product, no division
   const Real eken = O::half(fmx(q[IU], q[IU], q[IV] * q[IV]));
+  q[IP] = floor_prod(h.gm1 * fmx(-q[ID], eken, u[IP]), q[ID], h.smallp);
 #else
   const Real eken = O::half((q[IU] * q[IU]) + (q[IV] * q[IV]));
-#endif
   const Real e = O::div(u[IP], q[ID]) - eken;
   q[IP] = floor_prod((h.gm1 * q[ID]) * e, q[ID], h.smallp);
+#endif
 }
 
 // a and b the same number, bit for bit (an integer comparison).
@@ -248,8 +251,9 @@ __device__ __forceinline__ Real cell_invdt_q(const Hydro<Real>& h, const Real q[
   const Real vx = c + rabs(q[IU]);
   const Real vy = c + rabs(q[IV]);
 #if E2D_FMA_FORMS
-  // square cells: (vx + vy) / dx, one division (the FMA build's form)
-  if (same_bits(h.dx, h.dy)) return O::div(vx + vy, h.dx);
+  // square cells: (vx + vy) / dx as ((2c + |u|) + |v|) / dx, one division
+  // and two additions (the FMA build's form)
+  if (same_bits(h.dx, h.dy)) return O::div((O::twice(c) + rabs(q[IU])) + rabs(q[IV]), h.dx);
 #endif
   return O::div(vx, h.dx) + O::div(vy, h.dy);
 }
@@ -296,19 +300,6 @@ __device__ __forceinline__ bool prod_le0(double a, double b, bool& amb) {
 #endif
 }
 
-// dcen = 0.5*(qp - qm) of the limiter, from dl = q - qm and dr = qp - q.
-// The FMA build adds dl + dr: the same bits wherever both differences are
-// exact (neighbours within a factor of two of q, by Sterbenz's lemma), and
-// one FP64 addition fewer per slope; the exact build subtracts.
-template <typename Real>
-__device__ __forceinline__ Real slope_centre(Real qp, Real qm, Real dl, Real dr) {
-#if E2D_FMA_FORMS
-  return Ops<Real>::half(dl + dr);
-#else
-  return Ops<Real>::half(qp - qm);
-#endif
-}
-
 // Limiter cases recorded for the adjoint (3 bits per slope): bits 0-1 the
 // selection -- 0 limited to zero, 1 |dlft|, 2 |drgt|, 3 |dcen| -- and bit 2
 // set when the selected one-sided difference has the sign opposite to dcen.
@@ -320,7 +311,7 @@ __device__ __forceinline__ Real slope1(bool mc, Real q, Real qp, Real qm, bool& 
   const Real dl = q - qm, dr = qp - q;
   const Real dlft = mc ? O::twice(dl) : dl;
   const Real drgt = mc ? O::twice(dr) : dr;
-  const Real dcen = slope_centre(qp, qm, dl, dr);
+  const Real dcen = O::half(qp - qm);
   const Real al = rabs(dlft), ar = rabs(drgt);
   const Real slop = O::min(al, ar);
   bool zero;
