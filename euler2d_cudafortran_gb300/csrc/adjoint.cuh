@@ -228,12 +228,15 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
     vlb += lside ? vKb : 0.0; vrb += lside ? 0.0 : vKb;
     SLb = lside ? SKb : 0.0; SRb = lside ? 0.0 : SKb;
   }
-  // ptotstar and ustar = num / den
+  // ptotstar and ustar = num / den: d/drcr = (pl + rcl (ul - ur) - ptotstar,
+  // ur - ustar) / den and d/drcl = (pr + rcr (ul - ur) - ptotstar, ul -
+  // ustar) / den, where ptotstar = pl + rcl (ul - ustar) = pr + rcr (ustar -
+  // ur) (the HLLC star pressure from either side) reduces the two to
+  // (ustar - ur) pb and (ul - ustar) pa
   const double npb = O::div(ptotstarb, den), nub = O::div(ustarb, den);
-  double denb = -npb * ptotstar - nub * ustar;
-  double rcrb = npb * (pl + rcl * (ul - ur)) + nub * ur + denb;
-  double rclb = npb * (pr + rcr * (ul - ur)) + nub * ul + denb;
   const double pa = npb * rcr + nub, pb = npb * rcl - nub;
+  const double rcrb = (ustar - ur) * pb;
+  const double rclb = (ul - ustar) * pa;
   plb += pa;
   prb += pb;
   ulb += rcl * pa;   // npb rcl rcr + nub rcl
