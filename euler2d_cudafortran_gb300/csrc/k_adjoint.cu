@@ -504,13 +504,32 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
       if (!emul::gt_i(rec[HR_QL + ID], h.smallr)) qlb[ID] = 0.0;
       if (!emul::gt_i(rec[HR_QR + ID], h.smallr)) qrb[ID] = 0.0;
       const int nrm = xface ? 0 : 4;  // slope block of the face normal
+      // The slots start at zero and the passes run in order: pass 0 (even x
+      // faces) writes first to its cells' sums and x-slope slots, pass 2
+      // (even y faces) first to its cells' y-slope slots, so those writes
+      // are stores (0 + x is x: the same bits) and not additions.
+      if (pass == 0) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const double hl = Ops<double>::half(qlb[v]), hr = Ops<double>::half(qrb[v]);
-        sqb[v * NBOX + ka] += qlb[v];         // cell a's plus face (XMAX / YMAX)
-        sqb[v * NBOX + kb] += qrb[v];         // cell b's minus face
-        sra[(nrm + v) * NRING + a] += hl;
-        sra[(nrm + v) * NRING + b] -= hr;
+        for (int v = 0; v < 4; ++v) {
+          sqb[v * NBOX + ka] = qlb[v];
+          sqb[v * NBOX + kb] = qrb[v];
+          sra[v * NRING + a] = Ops<double>::half(qlb[v]);
+          sra[v * NRING + b] = Ops<double>::neg_if(Ops<double>::half(qrb[v]), true);
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const double hl = Ops<double>::half(qlb[v]), hr = Ops<double>::half(qrb[v]);
+          sqb[v * NBOX + ka] += qlb[v];         // cell a's plus face (XMAX / YMAX)
+          sqb[v * NBOX + kb] += qrb[v];         // cell b's minus face
+          if (pass == 2) {
+            sra[(nrm + v) * NRING + a] = hl;
+            sra[(nrm + v) * NRING + b] = Ops<double>::neg_if(hr, true);
+          } else {
+            sra[(nrm + v) * NRING + a] += hl;
+            sra[(nrm + v) * NRING + b] -= hr;
+          }
+        }
       }
     }
     __syncthreads();
