@@ -107,21 +107,26 @@ __device__ __forceinline__ void slope1_rev(bool mc, double q, double qp, double 
 }
 
 // The same from the forward step's recorded limiter case (3 bits, LIM_*):
-// nothing of the slope is recomputed.
+// nothing of the slope is recomputed.  It writes the neighbours' adjoints
+// (qpbar, qmbar set, not accumulated) and adds the cell's own to qbar: no
+// FP64 work for a slope limited to zero or a centred one, one addition for a
+// one-sided one, where accumulating into zero slots costs two.
 __device__ __forceinline__ void slope1_rev_case(bool mc, unsigned cs, double sb, double& qbar, double& qpbar,
                                                 double& qmbar) {
   const unsigned sel = cs & 3u;
+  qpbar = 0.0;
+  qmbar = 0.0;
   if (sel == LIM_ZERO) return;
   if (sel == LIM_CENTRE) {  // slope = dcen = (qp - qm) / 2
     const double g = O::half(sb);
-    qpbar += g;
-    qmbar -= g;
+    qpbar = g;
+    qmbar = O::neg_if(g, true);
     return;
   }
   const double g = O::neg_if(sb, (cs & LIM_FLIP) != 0u);  // dsgn * sign(x) * sb
   const double sg = mc ? O::twice(g) : g;                 // st * g
-  if (sel == LIM_LEFT) { qbar += sg; qmbar -= sg; }
-  else { qpbar += sg; qbar -= sg; }
+  if (sel == LIM_LEFT) { qbar += sg; qmbar = O::neg_if(sg, true); }
+  else { qpbar = sg; qbar -= sg; }
 }
 
 // trace_sources reverse: sb -> (qb, dqxb, dqyb).

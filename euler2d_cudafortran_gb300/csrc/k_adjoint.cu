@@ -565,7 +565,7 @@ __device__ __forceinline__ void step_rev_tile_tsq(const Hydro<double>& h, Field<
     const unsigned cases = (in && lim) ? tape.flag(tape.lim, gj, gi) : 0u;  // the forward's limiter cases
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      double qe = 0, qw = 0, qn = 0, qs = 0;
+      double qe, qw, qn, qs;
       adj::slope1_rev_case(mc, cases >> (3 * v), dqxb[v], qcb[v], qe, qw);
       adj::slope1_rev_case(mc, cases >> (12 + 3 * v), dqyb[v], qcb[v], qn, qs);
       sqb[v * NBOX + kc] += qcb[v];
