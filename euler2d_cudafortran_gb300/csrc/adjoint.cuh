@@ -23,7 +23,7 @@ __device__ __forceinline__ bool picks_first_max(double a, double b) { return emu
 __device__ __forceinline__ bool picks_first_min(double a, double b) { return emul::ord(a) < emul::ord(b); }
 
 // computePrimitives (serial_ref/m_utils.f90:35-64) reverse: qb (adjoint of
-// r, p, u, v) -> ub (adjoint of rho, E, rho u, rho v), given the forward
+// r, p, u, v) -> ub (adjoint of rho, E, rho u, rho v; written), given the forward
 // primitives q of the same cell (all four: r = q[ID], p = q[IP], u = q[IU],
 // v = q[IV]).  eos's pressure max((gm1 r) e, r smallp), e = E/r - eken,
 // returned its first operand exactly when p > r smallp (it returned p; the
@@ -45,21 +45,23 @@ __device__ __forceinline__ void primitives_rev_q(const Hydro<double>& h, const d
   // e = E/r - 0.5 (u^2 + v^2)
   double ubu = qb[IU] - eb * uu;
   double ubv = qb[IV] - eb * vv;
-  ub[IP] += O::div(eb, r);
+  ub[IP] = O::div(eb, r);
   rb -= O::div(eb * eu, r);
   // u = (rho u)/r, v = (rho v)/r
-  ub[IU] += O::div(ubu, r);
-  ub[IV] += O::div(ubv, r);
+  ub[IU] = O::div(ubu, r);
+  ub[IV] = O::div(ubv, r);
   rb -= O::div(ubu * uu + ubv * vv, r);
-  if (picks_first_max(u[ID], h.smallr)) ub[ID] += rb;
+  ub[ID] = picks_first_max(u[ID], h.smallr) ? rb : 0.0;
 }
 
-// The same, recomputing the primitives from u.
+// The same, recomputing the primitives from u, adding to ub.
 __device__ __forceinline__ void primitives_rev(const Hydro<double>& h, const double u[4], const double qb[4],
                                                double ub[4]) {
-  double q[4];
+  double q[4], t[4];
   primitives(h, u, q);
-  primitives_rev_q(h, u, q, qb, ub);
+  primitives_rev_q(h, u, q, qb, t);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) ub[v] += t[v];
 }
 
 // The compute_dt term of one cell (serial_ref/m_run.f90:278-281) reverse.
@@ -129,17 +131,17 @@ __device__ __forceinline__ void slope1_rev_case(bool mc, unsigned cs, double sb,
   else { qpbar = sg; qbar -= sg; }
 }
 
-// trace_sources reverse: sb -> (qb, dqxb, dqyb).
+// trace_sources reverse: sb -> (qb, dqxb, dqyb); qb is written (the cell's
+// adjoint starts here), dqxb and dqyb are added to.
 __device__ __forceinline__ void trace_sources_rev(const Hydro<double>& h, const double q[4], const double dqx[4],
                                                   const double dqy[4], const double sb[4], double qb[4],
                                                   double dqxb[4], double dqyb[4]) {
   const double r = q[ID], p = q[IP], u = q[IU], v = q[IV];
   const double div_ = dqx[IU] + dqy[IV];
-  qb[IU] -= sb[ID] * dqx[ID] + sb[IP] * dqx[IP] + sb[IU] * dqx[IU] + sb[IV] * dqx[IV];
-  qb[IV] -= sb[ID] * dqy[ID] + sb[IP] * dqy[IP] + sb[IU] * dqy[IU] + sb[IV] * dqy[IV];
-  qb[ID] -= sb[ID] * div_;
-  qb[ID] += O::div(O::div(sb[IU] * dqx[IP] + sb[IV] * dqy[IP], r), r);
-  qb[IP] -= sb[IP] * div_ * h.gamma0;
+  qb[IU] = -(sb[ID] * dqx[ID] + sb[IP] * dqx[IP] + sb[IU] * dqx[IU] + sb[IV] * dqx[IV]);
+  qb[IV] = -(sb[ID] * dqy[ID] + sb[IP] * dqy[IP] + sb[IU] * dqy[IU] + sb[IV] * dqy[IV]);
+  qb[ID] = O::div(O::div(sb[IU] * dqx[IP] + sb[IV] * dqy[IP], r), r) - sb[ID] * div_;
+  qb[IP] = -(sb[IP] * div_ * h.gamma0);
   dqxb[ID] -= sb[ID] * u;
   dqyb[ID] -= sb[ID] * v;
   dqxb[IP] -= sb[IP] * u + O::div(sb[IU], r);
