@@ -177,7 +177,7 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
 }
 
 // riemann_2d_hllc (serial_ref/m_utils.f90:534-644) reverse from the solve's
-// recorded forward values (riemann_hllc_rec): fb -> (qlb, qrb), "+=".
+// recorded forward values (riemann_hllc_rec): fb -> (qlb, qrb), written.
 __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, const double* rec, unsigned flags,
                                                      const double fb[4], double qlb[4], double qrb[4]) {
   const double ul = rec[HR_QL + IU], ur = rec[HR_QR + IU], vl = rec[HR_QL + IV], vr = rec[HR_QR + IV];
@@ -196,10 +196,13 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   const double uo = star ? ustar : uK, ptoto = star ? ptotstar : pK;
   const double den = rcr + rcl;
 
-  double rlb, rrb, plb, prb, ulb, urb, vlb = 0, vrb = 0, SLb, SRb, ustarb = 0, ptotstarb = 0;
+  // (Every adjoint below is written on its first contribution, not added to
+  // a zero: 0 + x costs an FP64 addition and gives the same bits, up to the
+  // sign of a zero.)
+  double rlb, rrb, plb, prb, ulb, urb, vlb, vrb, SLb, SRb, ustarb, ptotstarb;
   // flux[IV] = fr * (vl or vr)
   double frb = fb[ID] + fb[IV] * (vleft ? vl : vr);
-  if (vleft) vlb += fb[IV] * fr; else vrb += fb[IV] * fr;
+  const double fvb = fb[IV] * fr;
   // flux[IU] = fr * uo + ptoto ; flux[IP] = (etoto + ptoto) * uo
   double uob = fb[IU] * fr + fb[IP] * (etoto + ptoto);
   frb += fb[IU] * uo;
@@ -211,16 +214,19 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   {
     // one star state for either side: a warp whose faces sample both issues it once
     double rKb = rob, uKb = uob, pKb = ptotob, eKb = etotob, SKb = 0.0;
+    ustarb = 0.0;
+    ptotstarb = 0.0;
     if (star) {
       const double dS = SK - uK, d = SK - ustar;
-      ustarb += uob; ptotstarb += ptotob;
       const double rq = O::div(rob, d);
       rKb = rq * dS; SKb = rq * rK; uKb = O::neg_if(rq * rK, true);
       const double nEb = O::div(etotob, d);
       const double db = O::neg_if(rq * ro + nEb * etoto, true);
       SKb += nEb * eK; uKb -= nEb * eK; eKb = nEb * dS;
-      pKb = O::neg_if(nEb * uK, true); uKb -= nEb * pK; ptotstarb += nEb * ustar; ustarb += nEb * ptotstar;
-      SKb += db; ustarb -= db;
+      pKb = O::neg_if(nEb * uK, true); uKb -= nEb * pK;
+      ptotstarb = ptotob + nEb * ustar;
+      ustarb = (uob + nEb * ptotstar) - db;
+      SKb += db;
     }
     // etot_K = pK entho + hrK (uK uK + vK vK), hrK = rK / 2 (the other
     // side's energy is not sampled: its adjoint is zero)
@@ -232,8 +238,11 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
     rlb = lside ? rKb : 0.0; rrb = lside ? 0.0 : rKb;
     ulb = lside ? uKb : 0.0; urb = lside ? 0.0 : uKb;
     plb = lside ? pKb : 0.0; prb = lside ? 0.0 : pKb;
-    vlb += lside ? vKb : 0.0; vrb += lside ? 0.0 : vKb;
     SLb = lside ? SKb : 0.0; SRb = lside ? 0.0 : SKb;
+    // flux[IV]'s share to the side vleft names, vKb to side K
+    const double vsum = fvb + vKb;
+    vlb = vleft ? (lside ? vsum : fvb) : (lside ? vKb : 0.0);
+    vrb = vleft ? (lside ? 0.0 : vKb) : (lside ? fvb : vsum);
   }
   // ptotstar and ustar = num / den: d/drcr = (pl + rcl (ul - ur) - ptotstar,
   // ur - ustar) / den and d/drcl = (pr + rcr (ul - ur) - ptotstar, ul -
@@ -244,8 +253,11 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   const double pa = npb * rcr + nub, pb = npb * rcl - nub;
   const double rcrb = (ustar - ur) * pb;
   const double rclb = (ul - ustar) * pa;
-  plb += pa;
-  prb += pb;
+  {
+    const double pKt = (lside ? plb : prb) + (lside ? pa : pb);  // side K's pressure adjoint
+    plb = lside ? pKt : pa;
+    prb = lside ? pb : pKt;
+  }
   ulb += rcl * pa;   // npb rcl rcr + nub rcl
   urb -= rcr * pb;   // -npb rcl rcr + nub rcr
   // rcr = rr (SR - ur), rcl = rl (ul - SL)
@@ -260,16 +272,19 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
     const double rC = cmax_l ? rl : rr;
     const double cab = O::div(cmaxb, O::twice(cfC));
     const double pCb = O::div(cab * h.gamma0, rC), rCb = O::div(cab * caC, rC);
-    plb += cmax_l ? pCb : 0.0; prb += cmax_l ? 0.0 : pCb;
-    rlb -= cmax_l ? rCb : 0.0; rrb -= cmax_l ? 0.0 : rCb;
+    const double pCt = (cmax_l ? plb : prb) + pCb, rCt = (cmax_l ? rlb : rrb) - rCb;
+    plb = cmax_l ? pCt : plb; prb = cmax_l ? prb : pCt;
+    rlb = cmax_l ? rCt : rlb; rrb = cmax_l ? rrb : rCt;
   }
-  // pressure and density floors
-  if (pl_raw) qlb[IP] += plb; else rlb += plb * h.smallp;
-  if (pr_raw) qrb[IP] += prb; else rrb += prb * h.smallp;
-  if (emul::gt_i(rec[HR_QL + ID], h.smallr)) qlb[ID] += rlb;
-  if (emul::gt_i(rec[HR_QR + ID], h.smallr)) qrb[ID] += rrb;
-  qlb[IU] += ulb; qlb[IV] += vlb;
-  qrb[IU] += urb; qrb[IV] += vrb;
+  // pressure and density floors; the face-state adjoints are written
+  if (!pl_raw) rlb += plb * h.smallp;
+  if (!pr_raw) rrb += prb * h.smallp;
+  qlb[IP] = pl_raw ? plb : 0.0;
+  qrb[IP] = pr_raw ? prb : 0.0;
+  qlb[ID] = emul::gt_i(rec[HR_QL + ID], h.smallr) ? rlb : 0.0;
+  qrb[ID] = emul::gt_i(rec[HR_QR + ID], h.smallr) ? rrb : 0.0;
+  qlb[IU] = ulb; qlb[IV] = vlb;
+  qrb[IU] = urb; qrb[IV] = vrb;
 }
 
 // The same, recomputing the forward values from the face states; returns
