@@ -265,8 +265,16 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   rlb += rclb * (ul - SL); ulb += rclb * rl; SLb -= rclb * rl;
   // SR = max(ul, ur) + cmax, SL = min(ul, ur) - cmax
   const double cmaxb = SRb - SLb;
-  if (max_l) ulb += SRb; else urb += SRb;
-  if (min_l) ulb += SLb; else urb += SLb;
+  // (selected accumulators: one addition each, where branches cost a warp
+  // holding both cases two)
+  {
+    const double t = (max_l ? ulb : urb) + SRb;
+    ulb = max_l ? t : ulb; urb = max_l ? urb : t;
+  }
+  {
+    const double t = (min_l ? ulb : urb) + SLb;
+    ulb = min_l ? t : ulb; urb = min_l ? urb : t;
+  }
   // cmax = the faster side C's sound speed sqrt(max(gamma p / rho, smallc2))
   if (cmax_l ? cl_act : cr_act) {
     const double rC = cmax_l ? rl : rr;
