@@ -127,8 +127,10 @@ __device__ __forceinline__ void slope1_rev_case(bool mc, unsigned cs, double sb,
   }
   const double g = O::neg_if(sb, (cs & LIM_FLIP) != 0u);  // dsgn * sign(x) * sb
   const double sg = mc ? O::twice(g) : g;                 // st * g
-  if (sel == LIM_LEFT) { qbar += sg; qmbar = O::neg_if(sg, true); }
-  else { qpbar = sg; qbar -= sg; }
+  const bool left = sel == LIM_LEFT;                      // else LIM_RIGHT
+  qbar += O::neg_if(sg, !left);                           // one addition either way
+  qpbar = left ? 0.0 : sg;
+  qmbar = left ? O::neg_if(sg, true) : 0.0;
 }
 
 // trace_sources reverse: sb -> (qb, dqxb, dqyb); qb is written (the cell's
