@@ -191,8 +191,14 @@ __device__ __forceinline__ Real tile_compute(const Hydro<Real>& h, Real* base, i
     if constexpr (SQ) {
 #if E2D_FMA_FORMS
       // the FMA build keeps q + (s*dtdx)*0.5 for the faces (formed above
-      // unless the tape needed s itself)
-      if constexpr (TAPE) trace_qs(h, qc, dqx, dqy, Ops<Real>::half(dtdx), s);  // as the step without a tape
+      // unless the tape needed s itself).  trace_sources's s is -w and
+      // trace_qs forms fma(-dtdx/2, w, q) for the same fused w, which is
+      // fma(dtdx/2, s, q): the step without a tape's bits, from s
+      if constexpr (TAPE) {
+        const Real hdt = Ops<Real>::half(dtdx);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) s[v] = fmx(hdt, s[v], qc[v]);
+      }
 #else
 #pragma unroll
       for (int v = 0; v < 4; ++v) s[v] = Ops<Real>::half(s[v] * dtdx);
