@@ -197,6 +197,7 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   const double pK = lside ? pl : pr;
   const double uo = star ? ustar : uK, ptoto = star ? ptotstar : pK;
   const double den = rcr + rcl;
+  const double dsl = ul - SL, dsr = SR - ur;  // rcl = rl dsl, rcr = rr dsr
 
   // (Every adjoint below is written on its first contribution, not added to
   // a zero: 0 + x costs an FP64 addition and gives the same bits, up to the
@@ -219,7 +220,7 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
     ustarb = 0.0;
     ptotstarb = 0.0;
     if (star) {
-      const double dS = SK - uK, d = SK - ustar;
+      const double dS = lside ? O::neg_if(dsl, true) : dsr, d = SK - ustar;  // SK - uK
       const double rq = O::div(rob, d);
       rKb = rq * dS; SKb = rq * rK; uKb = O::neg_if(rq * rK, true);
       const double nEb = O::div(etotob, d);
@@ -263,8 +264,8 @@ __device__ __forceinline__ void riemann_hllc_rev_rec(const Hydro<double>& h, con
   ulb += rcl * pa;   // npb rcl rcr + nub rcl
   urb -= rcr * pb;   // -npb rcl rcr + nub rcr
   // rcr = rr (SR - ur), rcl = rl (ul - SL)
-  rrb += rcrb * (SR - ur); SRb += rcrb * rr; urb -= rcrb * rr;
-  rlb += rclb * (ul - SL); ulb += rclb * rl; SLb -= rclb * rl;
+  rrb += rcrb * dsr; SRb += rcrb * rr; urb -= rcrb * rr;
+  rlb += rclb * dsl; ulb += rclb * rl; SLb -= rclb * rl;
   // SR = max(ul, ur) + cmax, SL = min(ul, ur) - cmax
   const double cmaxb = SRb - SLb;
   // (selected accumulators: one addition each, where branches cost a warp

@@ -575,8 +575,9 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
   const Real cmax = O::max(cfastl, cfastr);
   const Real SL = O::min(ul, ur) - cmax;
   const Real SR = O::max(ul, ur) + cmax;
-  const Real rcl = rl * (ul - SL);
-  const Real rcr = rr * (SR - ur);
+  const Real dsl = ul - SL, dsr = SR - ur;
+  const Real rcl = rl * dsl;
+  const Real rcr = rr * dsr;
 #if E2D_FMA_FORMS
   const Real ustar = O::div(fmx(rcr, ur, fmx(rcl, ul, ptotl - ptotr)), rcr + rcl);
   const Real ptotstar = hllc_pstar(rcl, rcr, ul, ur, ptotl, ptotr, ustar);
@@ -607,11 +608,14 @@ __device__ __forceinline__ void riemann_hllc(const Hydro<Real>& h, const Real ql
     const Real ps = ptotstar * ustar;
     const Real d = lk ? ustar - SL : SR - ustar;
     ro = O::div(lk ? rcl : rcr, d);
-    etoto = O::div(fmx(lk ? ul - SL : SR - ur, etotk, fmx(O::neg_if(pk, !lk), uk, O::neg_if(ps, lk))), d);
+    etoto = O::div(fmx(lk ? dsl : dsr, etotk, fmx(O::neg_if(pk, !lk), uk, O::neg_if(ps, lk))), d);
 #else
+    // SL - ul is -(ul - SL) and rl (SL - ul) is -rcl, exactly (IEEE
+    // differences and products are odd in each operand): the reference's
+    // operands without forming them again
     const Real Sk = lk ? SL : SR;
-    const Real sk = Sk - uk;
-    ro = O::div(rk * sk, Sk - ustar);
+    const Real sk = lk ? O::neg_if(dsl, true) : dsr;
+    ro = O::div(lk ? O::neg_if(rcl, true) : rcr, Sk - ustar);
     etoto = O::div(((sk * etotk) - (pk * uk)) + (ptotstar * ustar), Sk - ustar);
 #endif
   }
@@ -660,8 +664,9 @@ __device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const d
   const bool min_l = pmin(ul, ur), max_l = pmax(ul, ur);
   const double SL = (min_l ? ul : ur) - cmax;
   const double SR = (max_l ? ul : ur) + cmax;
-  const double rcl = rl * (ul - SL);
-  const double rcr = rr * (SR - ur);
+  const double dsl = ul - SL, dsr = SR - ur;
+  const double rcl = rl * dsl;
+  const double rcr = rr * dsr;
 #if E2D_FMA_FORMS
   const double ustar = O::div(fmx(rcr, ur, fmx(rcl, ul, pl - pr)), rcr + rcl);
   const double ptotstar = hllc_pstar(rcl, rcr, ul, ur, pl, pr, ustar);
@@ -689,11 +694,14 @@ __device__ __forceinline__ void riemann_hllc_rec(const Hydro<double>& h, const d
     const double ps = ptotstar * ustar;
     const double d = lk ? ustar - SL : SR - ustar;
     ro = O::div(lk ? rcl : rcr, d);
-    etoto = O::div(fmx(lk ? ul - SL : SR - ur, etotk, fmx(O::neg_if(pk, !lk), uk, O::neg_if(ps, lk))), d);
+    etoto = O::div(fmx(lk ? dsl : dsr, etotk, fmx(O::neg_if(pk, !lk), uk, O::neg_if(ps, lk))), d);
 #else
+    // SL - ul is -(ul - SL) and rl (SL - ul) is -rcl, exactly (IEEE
+    // differences and products are odd in each operand): the reference's
+    // operands without forming them again
     const double Sk = lk ? SL : SR;
-    const double sk = Sk - uk;
-    ro = O::div(rk * sk, Sk - ustar);
+    const double sk = lk ? O::neg_if(dsl, true) : dsr;
+    ro = O::div(lk ? O::neg_if(rcl, true) : rcr, Sk - ustar);
     etoto = O::div(((sk * etotk) - (pk * uk)) + (ptotstar * ustar), Sk - ustar);
 #endif
   }
