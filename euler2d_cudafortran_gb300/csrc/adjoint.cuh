@@ -155,7 +155,8 @@ __device__ __forceinline__ void trace_sources_rev(const Hydro<double>& h, const 
   dqyb[IV] -= dd + sb[IV] * v;
 }
 
-// trace_face reverse: qfb -> (qb, dqb, sb) and the dt/d adjoint dtdb.
+// trace_face reverse: qfb -> (qb, dqb, sb; written) and the dt/d adjoint
+// dtdb (added to).
 // PRE: sh holds (s*dtd)*0.5 (dx == dy), and sb receives the adjoint of
 // (s*dtd) per unit dtd -- the caller multiplies the cell's sum by dtd once.
 template <bool PLUS, bool PRE = false>
@@ -169,11 +170,11 @@ __device__ __forceinline__ void trace_face_rev(const Hydro<double>& h, const dou
   // max(smallr, raw) returns raw unless smallr > raw: no gradient through the floor
   if (emul::gt_i(h.smallr, raw)) qfb[ID] = 0.0;
 #pragma unroll
-  for (int v = 0; v < 4; ++v) {
+  for (int v = 0; v < 4; ++v) {  // qb, dqb, sb written (their slots start here)
     const double hq = O::half(qfb[v]);
-    qb[v] += qfb[v];
-    dqb[v] += O::neg_if(hq, !PLUS);
-    sb[v] += PRE ? hq : dtd * hq;
+    qb[v] = qfb[v];
+    dqb[v] = O::neg_if(hq, !PLUS);
+    sb[v] = PRE ? hq : dtd * hq;
     dtdb += s[v] * hq;
   }
 }

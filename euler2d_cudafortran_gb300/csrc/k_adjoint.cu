@@ -240,8 +240,7 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
         double t = qlb[IU]; qlb[IU] = qlb[IV]; qlb[IV] = t;
         t = qrb[IU]; qrb[IU] = qrb[IV]; qrb[IV] = t;
       }
-      double qab[4] = {0, 0, 0, 0}, dqab[4] = {0, 0, 0, 0}, sab[4] = {0, 0, 0, 0};
-      double qbb[4] = {0, 0, 0, 0}, dqbb[4] = {0, 0, 0, 0}, sbb[4] = {0, 0, 0, 0};
+      double qab[4], dqab[4], sab[4], qbb[4], dqbb[4], sbb[4];
       // (a local accumulator: a reference selecting dtdxb or dtdyb would put
       // both in local memory)
       double dtdb = 0.0;
@@ -251,14 +250,33 @@ __device__ __forceinline__ void step_rev_tile(const Hydro<double>& h, Field<doub
       else dtdyb += dtdb;
       const int ka = ja * ABX + ia;
       const int kb = xface ? ka + 1 : ka + ABX;
+      // (pass 0 writes first to its cells' sums, x-slope and source slots,
+      // pass 2 to its cells' y-slope slots: stores, not additions to zero)
+      if (pass == 0) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        sqb[v * NBOX + ka] += qab[v];
-        sqb[v * NBOX + kb] += qbb[v];
-        sra[(nrm + v) * NRING + a] += dqab[v];
-        sra[(nrm + v) * NRING + b] += dqbb[v];
-        sra[(8 + v) * NRING + a] += sab[v];
-        sra[(8 + v) * NRING + b] += sbb[v];
+        for (int v = 0; v < 4; ++v) {
+          sqb[v * NBOX + ka] = qab[v];
+          sqb[v * NBOX + kb] = qbb[v];
+          sra[v * NRING + a] = dqab[v];
+          sra[v * NRING + b] = dqbb[v];
+          sra[(8 + v) * NRING + a] = sab[v];
+          sra[(8 + v) * NRING + b] = sbb[v];
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          sqb[v * NBOX + ka] += qab[v];
+          sqb[v * NBOX + kb] += qbb[v];
+          if (pass == 2) {
+            sra[(nrm + v) * NRING + a] = dqab[v];
+            sra[(nrm + v) * NRING + b] = dqbb[v];
+          } else {
+            sra[(nrm + v) * NRING + a] += dqab[v];
+            sra[(nrm + v) * NRING + b] += dqbb[v];
+          }
+          sra[(8 + v) * NRING + a] += sab[v];
+          sra[(8 + v) * NRING + b] += sbb[v];
+        }
       }
     }
     __syncthreads();
