@@ -225,3 +225,27 @@ def test_objective_before_gradient(e2d, oracle):
     assert abs(Jo - J2) <= 1e-13 * abs(J2) and abs(J1 - J2) <= 1e-13 * abs(J2)
     assert np.array_equal(d1, d2)
     assert float(np.sum(np.abs(g1 - g2)) / np.sum(np.abs(g2))) <= 1e-12
+
+
+@pytest.mark.parametrize("size", [(96, 80), (600, 520)], ids=["96x80", "600x520-carried"])
+def test_taping_forward_is_the_plain_forward(e2d, oracle, arith, size):
+    """With every state and tape kept, each step of the gradient's forward
+    sweep is the taping form of the step (it records the primitives, slopes,
+    sources and HLLC solves as it goes).  Its dt sequence -- each dt a
+    maximum over every cell of the state -- must equal bit for bit that of
+    the plain run through e2d_advance, in both builds: the recorded solve
+    returns riemann_hllc's flux, and the FMA build's taping step forms the
+    faces' cell values from the sources it records with the plain step's
+    bits.  At 600 x 520 the taping steps walk and carry tiles as the plain
+    persistent step does."""
+    nx, ny = size
+    p = e2d.make_params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann_solver=e2d.RIEMANN_HLLC,
+                        boundary_type_xmax=2, boundary_type_ymin=3, boundary_type_ymax=3)
+    po = oracle.Params(nx=nx, ny=ny, gamma0=1.4, cfl=0.8, riemann=2, bc_xmax=2, bc_ymin=3, bc_ymax=3)
+    u0 = generic_base(oracle, po)
+    n = 12
+    with e2d.Adjoint(p, arith=arith) as a:
+        _, _, dts = a.gradient(n, u0, dt_mode=0)
+        assert a.layout() == (n, True)
+    _, dts_plain = e2d.run_steps(n, p, u0=u0, arith=arith)
+    assert np.array_equal(np.asarray(dts, dtype=np.float64), np.asarray(dts_plain, dtype=np.float64))
